@@ -1,0 +1,243 @@
+/*
+ * tc.h -- C ABI of libtc, the GB300 (sm_103a) exact triangle-counting engine.
+ *
+ * The reference (KishantLab/TriangleCount) has no library API: its boundary is
+ * the command line and the whitespace-separated text formats of TC_128,
+ * wo_sort_tc_256 and round_clean_sg.  libtc keeps that contract in its CLIs
+ * and exposes the stages below as plain C entry points (plain pointers and
+ * sizes, no C++ or torch types) so that a cgo / JNI / ctypes binding can call
+ * them directly.  Each declaration names the reference code it replaces.
+ *
+ * Conventions
+ *  - Every function returns an int status: TC_OK (0) or a negative TC_E_*.
+ *    tc_last_error() gives a message for the calling thread's last failure.
+ *  - Host pointers are read during the call only; the caller keeps ownership.
+ *  - Library objects (contexts, graphs, batches, servers) are opaque handles
+ *    created and destroyed through this API.
+ *  - Device work of one context is ordered on that context's stream.  Calls
+ *    on distinct contexts may run from distinct host threads.
+ *  - Counts are exact unsigned 64-bit integers.
+ */
+#ifndef TC_H
+#define TC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define TC_API __attribute__((visibility("default")))
+#else
+#define TC_API
+#endif
+
+/* ---- status codes --------------------------------------------------------- */
+#define TC_OK 0
+#define TC_E_INVALID (-1)   /* bad argument or handle */
+#define TC_E_CUDA (-2)      /* CUDA runtime error */
+#define TC_E_NOMEM (-3)     /* host/device allocation failed or over budget */
+#define TC_E_RANGE (-4)     /* value does not fit the device index type */
+#define TC_E_FORMAT (-5)    /* malformed file or CSR (unsorted row, bad id) */
+#define TC_E_IO (-6)        /* file cannot be opened, read or written */
+#define TC_E_NOT_READY (-7) /* asynchronous result not available yet */
+#define TC_E_TIMEOUT (-8)   /* bounded wait expired */
+#define TC_E_NO_DEVICE (-9) /* no CUDA device / device index out of range */
+#define TC_E_STATE (-10)    /* object is in the wrong state for the call */
+
+/* Orientation tie-break for vertices of equal degree.
+ * TC_TIE_REFERENCE keeps u->w iff deg u < deg w, or deg u == deg w and w < u
+ *   (Med_dataset/without_part_preprocess.py:37-50, round_clean_subgraph.cu:180-201).
+ * TC_TIE_ID_ASC keeps u->w iff (deg u, u) < (deg w, w).
+ * Both orient every edge once; counts are identical, files differ. */
+#define TC_TIE_REFERENCE 0
+#define TC_TIE_ID_ASC 1
+
+typedef struct tc_ctx tc_ctx;       /* device + stream + scratch pool */
+typedef struct tc_graph tc_graph;   /* device-resident oriented CSR, int32 */
+typedef struct tc_ugraph tc_ugraph; /* device-resident undirected CSR, int32 */
+typedef struct tc_batch tc_batch;   /* many graphs, one persistent launch */
+typedef struct tc_server tc_server; /* continuous-batching request loop */
+
+/* ---- errors, version ------------------------------------------------------ */
+/* Replaces the reference's printf + exit(0) on failure
+ * (ShareKernelTCV62_update_v1.cu:200-203, without_sorting_tc.cu:234-238). */
+TC_API const char *tc_last_error(void);
+TC_API const char *tc_status_string(int status);
+TC_API int tc_version(void); /* major*10000 + minor*100 + patch */
+
+/* ---- context -------------------------------------------------------------- */
+/* Replaces cudaSetDevice(0) and the default stream of the reference drivers
+ * (without_sorting_tc.cu:226).  The context owns a non-blocking stream and a
+ * device scratch pool reused across calls (the reference cudaMallocs inside
+ * its timed loop, ShareKernelTCV62_update_v1.cu:254-261, 271-275). */
+TC_API int tc_ctx_create(int device, tc_ctx **out);
+TC_API int tc_ctx_destroy(tc_ctx *ctx);
+/* Use an external cudaStream_t (passed as void*) instead of the own stream. */
+TC_API int tc_ctx_set_stream(tc_ctx *ctx, void *cuda_stream);
+TC_API void *tc_ctx_get_stream(tc_ctx *ctx);
+TC_API int tc_ctx_synchronize(tc_ctx *ctx);
+TC_API int tc_ctx_device_info(tc_ctx *ctx, int *sm_count, size_t *free_bytes, size_t *total_bytes);
+
+/* Strategy thresholds of the counting kernel (picked by the autotuner).
+ * Roots u with 2 <= d+(u) <= warp_max_deg are counted by one warp with a
+ * shared-memory hash of N+(u); larger roots are split into block units of
+ * block_slice out-neighbours, each probing a shared hash of one tile of N+(u).
+ * Roots with d+(u) <= tiny_max_deg use a register-broadcast compare instead of
+ * the hash.  In tc_ctx_set_tuning, warp_max_deg / block_slice <= 0 and
+ * tiny_max_deg / blocks_per_sm < 0 keep the current value. */
+typedef struct tc_tuning {
+    int32_t warp_max_deg;   /* 32..1024, power of two */
+    int32_t block_slice;    /* out-neighbours per block unit, multiple of 32 */
+    int32_t tiny_max_deg;   /* 0..32 */
+    int32_t blocks_per_sm;  /* persistent grid = SMs * this (0: occupancy) */
+} tc_tuning;
+TC_API int tc_ctx_get_tuning(tc_ctx *ctx, tc_tuning *out);
+TC_API int tc_ctx_set_tuning(tc_ctx *ctx, const tc_tuning *in);
+
+/* ---- oriented graphs ------------------------------------------------------ */
+/* Upload an oriented CSR: n_rows rows, row_ptr[n_rows+1], col[nnz], rows
+ * strictly ascending, ids in [0, n_rows).  Roots are rows [0, n_roots); the
+ * unpartitioned file has n_roots == n_rows, a halo part has n_roots = t_ver.
+ * Replaces the fscanf + cudaMemcpy of ShareKernelTCV62_update_v1.cu:207-239
+ * (int32) and without_sorting_tc.cu:250-329 (u64, narrowed to int32 here;
+ * TC_E_RANGE when nnz or an id does not fit).  The rows are validated on the
+ * device; an unsorted or out-of-range row gives TC_E_FORMAT. */
+TC_API int tc_graph_upload_i32(tc_ctx *ctx, const int32_t *row_ptr, const int32_t *col, int64_t n_rows,
+                               int64_t nnz, int64_t n_roots, tc_graph **out);
+TC_API int tc_graph_upload_u64(tc_ctx *ctx, const uint64_t *row_ptr, const uint64_t *col, int64_t n_rows,
+                               int64_t nnz, int64_t n_roots, tc_graph **out);
+/* Wrap caller-owned device arrays without copying (no validation). */
+TC_API int tc_graph_wrap_device_i32(tc_ctx *ctx, const int32_t *d_row_ptr, const int32_t *d_col, int64_t n_rows,
+                                    int64_t nnz, int64_t n_roots, tc_graph **out);
+TC_API int tc_graph_info(const tc_graph *g, int64_t *n_rows, int64_t *nnz, int64_t *n_roots);
+TC_API int tc_graph_download_i32(tc_ctx *ctx, const tc_graph *g, int32_t *row_ptr, int32_t *col);
+TC_API int tc_graph_destroy(tc_graph *g);
+
+/* ---- counting: one graph per launch (the drop-in path) -------------------- */
+typedef struct tc_count_stats {
+    float count_ms;     /* device time of the counting kernels ("Search") */
+    float finalize_ms;  /* device time of the result read-back ("Sum_result") */
+    int32_t launches;   /* kernels launched by this call */
+    int32_t heavy_units;/* block units produced by the classifier */
+} tc_count_stats;
+
+/* Exact triangle count of g: sum over roots u of
+ * sum_{v in N+(u)} |N+(u) n N+(v)|.  Replaces Find_Triangle<<<V,128>>> +
+ * cub::DeviceReduce::Sum (ShareKernelTCV62_update_v1.cu:43-191, 263-282) and
+ * the u64 twin (without_sorting_tc.cu:57-219, 399-434).  Blocks until the
+ * result is on the host.  stats may be NULL. */
+TC_API int tc_count(tc_ctx *ctx, tc_graph *g, uint64_t *out, tc_count_stats *stats);
+/* Enqueue the count of g on the context stream; the result lands in the
+ * 8-byte device word d_out (overwritten).  Returns without synchronising. */
+TC_API int tc_count_async(tc_ctx *ctx, tc_graph *g, uint64_t *d_out);
+/* Per-root counts, the reference's g_sum[u] (ShareKernelTCV62_update_v1.cu:175-186):
+ * per_root[u] for u in [0, n_roots), host array. */
+TC_API int tc_count_per_root(tc_ctx *ctx, tc_graph *g, uint64_t *per_root, uint64_t *total);
+/* End-to-end: host CSR in, count out (upload + validate + count + read-back). */
+TC_API int tc_count_csr_i32(tc_ctx *ctx, const int32_t *row_ptr, const int32_t *col, int64_t n_rows, int64_t nnz,
+                            uint64_t *out);
+
+/* ---- batched counting: many graphs or parts, one persistent launch --------- */
+/* Replaces the sequential per-part loop of without_sorting_tc.cu:244-465 (one
+ * launch + host sync per part).  A batch holds the descriptor table of its
+ * graphs and a CUDA graph of [classify -> persistent count]; tc_batch_run
+ * replays it and writes outs[i] for graphs[i].  Graphs must outlive the batch. */
+TC_API int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n_graphs, tc_batch **out);
+TC_API int tc_batch_run(tc_batch *b, uint64_t *outs);
+TC_API int tc_batch_run_async(tc_batch *b);             /* enqueue only */
+TC_API int tc_batch_results(tc_batch *b, uint64_t *outs); /* sync + read back */
+TC_API int tc_batch_destroy(tc_batch *b);
+/* Per-graph launches of the same kernels with a sync after each graph: the
+ * plain path the batch is compared against. */
+TC_API int tc_count_each(tc_ctx *ctx, tc_graph *const *graphs, int n_graphs, uint64_t *outs);
+
+/* ---- device preprocessing ---------------------------------------------------- */
+/* Edge list -> simple undirected CSR on the device: drop self-loops,
+ * symmetrise, dedupe (64-bit key radix sort + unique), drop isolated vertices
+ * with an order-preserving relabel, rows ascending.  Replaces dgl
+ * remove_self_loop / to_bidirected / remove_nodes / adj_tensors
+ * (Med_dataset/without_part_preprocess.py:193-228).  n_nodes: vertex count
+ * hint (max id + 1 is used when larger).  Ids must be < 2^31. */
+TC_API int tc_ugraph_from_edges(tc_ctx *ctx, const int64_t *src, const int64_t *dst, int64_t n_edges,
+                                int64_t n_nodes, tc_ugraph **out);
+/* Upload an undirected CSR (e.g. a _part.csr file, Halo_creation_preprocess.py:259-278).
+ * deg may be NULL (row lengths are used); otherwise it is the file's degree
+ * column used by the halo orientation (round_clean_subgraph.cu:172, 178). */
+TC_API int tc_ugraph_upload_i64(tc_ctx *ctx, const int64_t *row_ptr, const int64_t *col, const int64_t *deg,
+                                int64_t n_rows, int64_t nnz, tc_ugraph **out);
+TC_API int tc_ugraph_info(const tc_ugraph *g, int64_t *n_rows, int64_t *nnz);
+TC_API int tc_ugraph_download(tc_ctx *ctx, const tc_ugraph *g, int64_t *row_ptr, int64_t *col, int64_t *deg);
+TC_API int tc_ugraph_destroy(tc_ugraph *g);
+/* Degree orientation on the device: count -> scan -> stable scatter.
+ * Replaces Find_size / cp.cumsum / Convert (without_part_preprocess.py:19-111, 253-270). */
+TC_API int tc_orient(tc_ctx *ctx, const tc_ugraph *ug, int tie, tc_graph **out);
+/* Edge list straight to an oriented graph (tc_ugraph_from_edges + tc_orient). */
+TC_API int tc_graph_from_edges(tc_ctx *ctx, const int64_t *src, const int64_t *dst, int64_t n_edges, int64_t n_nodes,
+                               int tie, tc_graph **out);
+
+/* ---- halo partitions ---------------------------------------------------------- */
+/* Per-part halo subgraphs on the device.  For each part p in [0, k): part
+ * vertices (ascending) then their 1-hop halo (ascending) get local ids; the
+ * oriented edges among them are kept with rows ascending; halo vertices with
+ * zero in-degree are pruned until none is left.  parts_out[p] is an oriented
+ * graph with n_roots = t_ver.  part[] is a host array of n_rows ints in [0,k).
+ * Replaces create_subgraph_with_halo (round_clean_subgraph.cu:357-902) with
+ * the prune of Halo_creation_preprocess.py:566-589. */
+TC_API int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k, int tie,
+                           tc_graph **parts_out);
+
+/* ---- host utilities: text files (the reference's on-disk contract) -------- */
+/* Parse a whitespace-separated file of unsigned integers into a flat array,
+ * in file order, as the reference's fscanf loops read it
+ * (ShareKernelTCV62_update_v1.cu:207-230, without_sorting_tc.cu:242-286,
+ * round_clean_subgraph.cu:924-968).  Multi-threaded.  *data is malloc'd by
+ * the library; release it with tc_host_free. */
+TC_API int tc_text_read_u64(const char *path, uint64_t **data, int64_t *n);
+TC_API void tc_host_free(void *p);
+/* Append one line of n signed values of elem_bytes (4: int32, 8: int64) to the
+ * file; mode 'w' truncates first.  trailing_space != 0 writes "v0 v1 ... vn-1 \n"
+ * (every value followed by a space, as without_part_preprocess.py:306-311 and
+ * round_clean_subgraph.cu:850-865 write arrays); 0 writes "v0 v1 ... vn-1\n"
+ * (round_clean_subgraph.cu:371 header lines). */
+TC_API int tc_text_write_line(const char *path, const void *values, int64_t n, int elem_bytes, char mode,
+                              int trailing_space);
+/* Page-locked host memory for fast transfers (cudaMallocHost). */
+TC_API int tc_host_alloc_pinned(size_t bytes, void **out);
+TC_API int tc_host_free_pinned(void *p);
+/* Binary CSR cache (.tcsr): header + int64 row_ptr + int32 col. */
+TC_API int tc_tcsr_write(const char *path, const int64_t *row_ptr, const int32_t *col, int64_t n_rows,
+                         int64_t nnz, int64_t n_roots, int64_t aux);
+TC_API int tc_tcsr_read_header(const char *path, int64_t *n_rows, int64_t *nnz, int64_t *n_roots, int64_t *aux);
+TC_API int tc_tcsr_read(const char *path, int64_t *row_ptr, int32_t *col);
+
+/* ---- host utilities: seeded synthetic graphs -------------------------------- */
+/* R-MAT: n = edge_factor << scale sampled edges, quadrant probabilities
+ * (a, b, c, 1-a-b-c), then a seeded vertex permutation when permute != 0. */
+TC_API int tc_gen_rmat(int scale, int edge_factor, double a, double b, double c, uint64_t seed, int permute,
+                       int64_t *src, int64_t *dst);
+/* Road-like planar graph on a width x height grid: 4-neighbour edges each
+ * deleted with probability p_delete, plus one random diagonal per cell with
+ * probability diag_rate.  Returns the edge count via *n_edges; buffers must
+ * hold 3*width*height edges. */
+TC_API int tc_gen_road(int64_t width, int64_t height, double p_delete, double diag_rate, uint64_t seed,
+                       int64_t *src, int64_t *dst, int64_t *n_edges);
+/* Erdos-Renyi with mean degree p*(n-1): M = round(p*n*(n-1)/2) uniform vertex
+ * pairs (G(n, M); repeats and self-loops go in clean-up).  *n_edges: buffer
+ * capacity in, M out. */
+TC_API int tc_gen_er(int64_t n, double p, uint64_t seed, int64_t *src, int64_t *dst, int64_t *n_edges);
+/* Chung-Lu: expected degrees w_i ~ (i+1)^(-1/(gamma-1)) scaled to mean
+ * avg_deg and capped at sqrt(n*avg_deg) (= sqrt(2E)); n*avg_deg/2 edges with
+ * endpoints drawn proportional to w. */
+TC_API int tc_gen_chung_lu(int64_t n, double gamma, double avg_deg, uint64_t seed, int64_t *src, int64_t *dst,
+                           int64_t n_edges);
+/* Seeded uniform part assignment in [0, k) (replaces the unseeded
+ * np.random.randint, Halo_creation_preprocess.py:288, 325, 362). */
+TC_API int tc_gen_parts_random(int64_t n, int k, uint64_t seed, int32_t *part);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TC_H */

@@ -1,0 +1,52 @@
+// ref_launch.cu -- TEST INFRASTRUCTURE ONLY: launches the reference's own
+// TC_128 kernel (Find_Triangle of src/WithoutPartition/ShareKernelTCV62_update_v1.cu:43-191),
+// compiled from the reference sources into oracle/_ref/tc128_sm103a.cubin by
+// oracle/build_ref.sh, with the reference's launch shape (one 128-thread block
+// per vertex, :264).  Used by the tests to cross-check per-root counts and by
+// bench.py to time the reference kernel on the same GPU.  Host code only.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+extern "C" {
+
+// Returns 0 on success; per_root[V] receives g_sum, *ms the kernel time of
+// the last of `runs` launches (events around the launch, as :263-265).
+int ref_tc128_run(const char *cubin, const int32_t *rp, const int32_t *col, int32_t V, int32_t nnz, int runs,
+                  uint64_t *per_root, float *ms, char *err, int err_len) {
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t k = nullptr;
+    int32_t *d_rp = nullptr, *d_col = nullptr;
+    unsigned long long *d_sum = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaLibraryLoadFromFile(&lib, cubin, nullptr, nullptr, 0, nullptr, nullptr, 0);
+    if (e == cudaSuccess) e = cudaLibraryGetKernel(&k, lib, "_Z13Find_TrianglePiS_iiPy");
+    if (e == cudaSuccess) e = cudaMalloc(&d_rp, sizeof(int32_t) * ((size_t)V + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&d_col, sizeof(int32_t) * (size_t)(nnz ? nnz : 1));
+    if (e == cudaSuccess) e = cudaMalloc(&d_sum, sizeof(unsigned long long) * (size_t)(V ? V : 1));
+    if (e == cudaSuccess) e = cudaMemcpy(d_rp, rp, sizeof(int32_t) * ((size_t)V + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && nnz) e = cudaMemcpy(d_col, col, sizeof(int32_t) * (size_t)nnz, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    int edges = 0;  // the kernel's unused `edge` argument
+    for (int r = 0; r < runs && e == cudaSuccess && V > 0; ++r) {
+        void *args[] = {&d_col, &d_rp, &V, &edges, &d_sum};
+        e = cudaEventRecord(e0);
+        if (e == cudaSuccess) e = cudaLaunchKernel((const void *)k, dim3((unsigned)V), dim3(128), args, 0, nullptr);
+        if (e == cudaSuccess) e = cudaEventRecord(e1);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+    }
+    if (e == cudaSuccess && V > 0)
+        e = cudaMemcpy(per_root, d_sum, sizeof(unsigned long long) * (size_t)V, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess && err) snprintf(err, (size_t)err_len, "%s", cudaGetErrorString(e));
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(d_rp);
+    cudaFree(d_col);
+    cudaFree(d_sum);
+    if (lib) cudaLibraryUnload(lib);
+    return e == cudaSuccess ? 0 : (int)e;
+}
+
+}  // extern "C"

@@ -1,0 +1,127 @@
+"""GPU counting kernels against the oracle and closed-form counts (bit-exact)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import families
+import oracle
+import trianglecount_gb300 as tc
+from trianglecount_gb300 import generators as gen
+
+pytestmark = pytest.mark.gpu
+
+TUNINGS = [
+    {},  # defaults
+    {"warp_max_deg": 32, "block_slice": 32, "tiny_max_deg": 0},   # heavy path everywhere, tiny slices
+    {"warp_max_deg": 1024, "block_slice": 2048, "tiny_max_deg": 32},
+    {"warp_max_deg": 64, "block_slice": 96, "tiny_max_deg": 4, "blocks_per_sm": 1},
+]
+
+
+@pytest.fixture
+def tuned(ctx):
+    old = ctx.get_tuning()
+    yield ctx
+    ctx.set_tuning(old["warp_max_deg"], old["block_slice"], old["tiny_max_deg"], 0)
+
+
+@pytest.mark.parametrize("tuning", TUNINGS)
+def test_known_graphs(tuned, golden_dir, tuning):
+    tuned.set_tuning(**tuning)
+    for c in json.load(open(os.path.join(golden_dir, "known_graphs.json"))):
+        src, dst, n = families.build(c["family"], c["args"])
+        orp, ocl, _ = oracle.pipeline(src, dst, n)
+        g = tuned.upload(orp, ocl)
+        assert tuned.count(g) == c["expected"], (c["family"], c["args"], tuning)
+
+
+@pytest.mark.parametrize("tuning", TUNINGS)
+@pytest.mark.parametrize("scale", [8, 11, 14])
+def test_rmat_per_root_matches_oracle(tuned, tuning, scale):
+    tuned.set_tuning(**tuning)
+    src, dst = gen.rmat(scale)
+    orp, ocl, want = oracle.pipeline(src, dst)
+    _, want_pr = oracle.count(orp, ocl, per_root=True)
+    g = tuned.upload(orp, ocl)
+    got_pr = tuned.count_per_root(g)
+    assert np.array_equal(got_pr, want_pr)
+    assert tuned.count(g) == want
+
+
+@pytest.mark.parametrize("tie", ["reference", "id_asc"])
+@pytest.mark.parametrize("maker", ["rmat16", "road", "er", "chung_lu", "complete_1500"])
+def test_graph_families_match_oracle(ctx, maker, tie):
+    if maker == "rmat16":
+        src, dst = gen.rmat(16)
+    elif maker == "road":
+        src, dst = gen.road(300)
+    elif maker == "er":
+        src, dst = gen.er(50000, 40.0, seed=9)
+    elif maker == "chung_lu":
+        src, dst = gen.chung_lu(200000, 16.0, seed=10)
+    else:
+        src, dst, _ = families.complete(1500)
+    orp, ocl, want = oracle.pipeline(src, dst, tie=tie)
+    g = ctx.upload(orp, ocl)
+    got, st = ctx.count(g, stats=True)
+    assert got == want
+    assert st["launches"] == 2 and st["count_ms"] > 0
+
+
+def test_rmat_golden_counts_on_device(ctx, golden_dir):
+    for c in json.load(open(os.path.join(golden_dir, "rmat_counts.json"))):
+        src, dst = gen.rmat(c["scale"], 16, seed=c["seed"])
+        g = ctx.graph_from_edges(src, dst)
+        assert (g.n_rows, g.nnz) == (c["V"], c["oriented_nnz"])
+        assert ctx.count(g) == c["triangles"]
+
+
+def test_halo_style_roots_subset(ctx):
+    """n_roots < n_rows: only rows [0, n_roots) are roots (wo_sort_tc_256's t_ver)."""
+    src, dst = gen.rmat(12)
+    orp, ocl, _ = oracle.pipeline(src, dst)
+    for nr in (0, 1, 100, len(orp) // 2, len(orp) - 1):
+        g = ctx.upload(orp, ocl, n_roots=nr)
+        assert ctx.count(g) == oracle.count(orp, ocl, n_roots=nr)
+
+
+def test_edge_cases(ctx):
+    # no vertices
+    g = ctx.upload(np.zeros(1, np.int32), np.zeros(0, np.int32))
+    assert ctx.count(g) == 0
+    assert len(ctx.count_per_root(g)) == 0
+    # vertices, no edges
+    g = ctx.upload(np.zeros(6, np.int32), np.zeros(0, np.int32))
+    assert ctx.count(g) == 0
+    # one triangle 0->1, 0->2, 1->2
+    g = ctx.upload(np.array([0, 2, 3, 3], np.int32), np.array([1, 2, 2], np.int32))
+    assert ctx.count(g) == 1 and list(ctx.count_per_root(g)) == [1, 0, 0]
+    # u64 upload path (the partitioned file's integer width)
+    g = ctx.upload(np.array([0, 2, 3, 3], np.uint64), np.array([1, 2, 2], np.uint64))
+    assert ctx.count(g) == 1
+
+
+def test_invalid_csr_is_rejected(ctx):
+    bad_order = (np.array([0, 2, 3, 3], np.int32), np.array([2, 1, 2], np.int32))
+    bad_dup = (np.array([0, 2, 3, 3], np.int32), np.array([1, 1, 2], np.int32))
+    bad_id = (np.array([0, 2, 3, 3], np.int32), np.array([1, 7, 2], np.int32))
+    bad_rp = (np.array([0, 3, 2, 3], np.int32), np.array([1, 2, 2], np.int32))
+    for rp, col in (bad_order, bad_dup, bad_id, bad_rp):
+        with pytest.raises(tc.TCError) as e:
+            ctx.upload(rp, col)
+        assert e.value.code == "TC_E_FORMAT"
+    with pytest.raises(tc.TCError) as e:
+        ctx.upload(np.array([0, 1, 1], np.uint64), np.array([2**33], np.uint64))
+    assert e.value.code == "TC_E_RANGE"
+    with pytest.raises(tc.TCError):
+        ctx.set_tuning(warp_max_deg=100)
+
+
+def test_end_to_end_host_csr_and_repeatability(ctx):
+    src, dst = gen.rmat(15)
+    orp, ocl, want = oracle.pipeline(src, dst)
+    assert ctx.count_csr(orp, ocl) == want
+    g = ctx.upload(orp, ocl)
+    assert {ctx.count(g) for _ in range(5)} == {want}

@@ -1,0 +1,294 @@
+"""Python host side of libtc: contexts, device graphs, counting, batching,
+preprocessing and halo extraction.  Thin wrappers over the C ABI; every
+computation runs in libtc's CUDA kernels.
+
+The operations mirror the reference's processing stages:
+
+  Context.ugraph_from_edges  ~ without_part_preprocess.py:193-228 (DGL clean-up)
+  Context.orient             ~ without_part_preprocess.py:19-111 (Find_size/Convert)
+  Context.upload + count     ~ TC_128 (ShareKernelTCV62_update_v1.cu:192-310)
+  Context.halo_extract       ~ round_clean_sg (round_clean_subgraph.cu:357-902)
+  Batch / Context.count_each ~ wo_sort_tc_256's per-part loop (without_sorting_tc.cu:244-465)
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from . import _native as N
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _tie(tie) -> int:
+    if isinstance(tie, str):
+        return N.TIE[tie]
+    return int(tie)
+
+
+class Graph:
+    """A device-resident oriented CSR (int32).  Roots are rows [0, n_roots)."""
+
+    def __init__(self, ctx: "Context", handle: C.c_void_p):
+        self.ctx = ctx
+        self._h = handle
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise ValueError("graph already freed")
+        return self._h
+
+    def info(self) -> tuple[int, int, int]:
+        r, n, k = C.c_int64(), C.c_int64(), C.c_int64()
+        N.call("tc_graph_info", self.handle, C.byref(r), C.byref(n), C.byref(k))
+        return r.value, n.value, k.value
+
+    @property
+    def n_rows(self) -> int:
+        return self.info()[0]
+
+    @property
+    def nnz(self) -> int:
+        return self.info()[1]
+
+    @property
+    def n_roots(self) -> int:
+        return self.info()[2]
+
+    def download(self) -> tuple[np.ndarray, np.ndarray]:
+        n_rows, nnz, _ = self.info()
+        rp = np.empty(n_rows + 1, np.int32)
+        col = np.empty(nnz, np.int32)
+        N.call("tc_graph_download_i32", self.ctx.handle, self.handle, _ptr(rp), _ptr(col))
+        return rp, col
+
+    def count(self) -> int:
+        return self.ctx.count(self)
+
+    def free(self) -> None:
+        if self._h is not None:
+            N.lib().tc_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class UGraph:
+    """A device-resident simple undirected CSR (int32) with its degree column."""
+
+    def __init__(self, ctx: "Context", handle: C.c_void_p):
+        self.ctx = ctx
+        self._h = handle
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise ValueError("graph already freed")
+        return self._h
+
+    def info(self) -> tuple[int, int]:
+        r, n = C.c_int64(), C.c_int64()
+        N.call("tc_ugraph_info", self.handle, C.byref(r), C.byref(n))
+        return r.value, n.value
+
+    def download(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        n_rows, nnz = self.info()
+        rp = np.empty(n_rows + 1, np.int64)
+        col = np.empty(nnz, np.int64)
+        deg = np.empty(n_rows, np.int64)
+        N.call("tc_ugraph_download", self.ctx.handle, self.handle, _ptr(rp), _ptr(col), _ptr(deg))
+        return rp, col, deg
+
+    def free(self) -> None:
+        if self._h is not None:
+            N.lib().tc_ugraph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many graphs counted by one persistent launch, replayed as a CUDA graph."""
+
+    def __init__(self, ctx: "Context", graphs: Sequence[Graph]):
+        self.ctx = ctx
+        self.graphs = list(graphs)  # keeps the graphs alive
+        arr = (C.c_void_p * len(self.graphs))(*[g.handle for g in self.graphs])
+        h = C.c_void_p()
+        N.call("tc_batch_create", ctx.handle, arr, len(self.graphs), C.byref(h))
+        self._h = h
+        self._out = np.empty(len(self.graphs), np.uint64)
+
+    def run(self) -> np.ndarray:
+        N.call("tc_batch_run", self._h, _ptr(self._out))
+        return self._out.copy()
+
+    def run_async(self) -> None:
+        N.call("tc_batch_run_async", self._h)
+
+    def results(self) -> np.ndarray:
+        N.call("tc_batch_results", self._h, _ptr(self._out))
+        return self._out.copy()
+
+    def free(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            N.lib().tc_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Context:
+    """A CUDA device, a stream and libtc's scratch pool."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        N.call("tc_ctx_create", int(device), C.byref(h))
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            N.lib().tc_ctx_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- device / stream / tuning ----
+    @property
+    def stream(self) -> int:
+        return N.lib().tc_ctx_get_stream(self._h) or 0
+
+    def set_stream(self, stream_ptr: int) -> None:
+        N.call("tc_ctx_set_stream", self._h, C.c_void_p(stream_ptr))
+
+    def synchronize(self) -> None:
+        N.call("tc_ctx_synchronize", self._h)
+
+    def device_info(self) -> dict:
+        sm, f, t = C.c_int(), C.c_size_t(), C.c_size_t()
+        N.call("tc_ctx_device_info", self._h, C.byref(sm), C.byref(f), C.byref(t))
+        return {"sm_count": sm.value, "free_bytes": f.value, "total_bytes": t.value}
+
+    def get_tuning(self) -> dict:
+        t = N.Tuning()
+        N.call("tc_ctx_get_tuning", self._h, C.byref(t))
+        return {k: getattr(t, k) for k, _ in N.Tuning._fields_}
+
+    def set_tuning(self, warp_max_deg: int = 0, block_slice: int = 0, tiny_max_deg: int = -1,
+                   blocks_per_sm: int = -1) -> None:
+        t = N.Tuning(warp_max_deg, block_slice, tiny_max_deg, blocks_per_sm)
+        N.call("tc_ctx_set_tuning", self._h, C.byref(t))
+
+    # ---- graphs ----
+    def upload(self, row_ptr: np.ndarray, col: np.ndarray, n_roots: int | None = None) -> Graph:
+        """Upload an oriented CSR (int32, or u64 narrowed on the device)."""
+        n_rows = len(row_ptr) - 1
+        n_roots = n_rows if n_roots is None else int(n_roots)
+        h = C.c_void_p()
+        if row_ptr.dtype in (np.uint64, np.int64):
+            rp = np.ascontiguousarray(row_ptr, np.uint64)
+            cl = np.ascontiguousarray(col, np.uint64)
+            N.call("tc_graph_upload_u64", self._h, _ptr(rp), _ptr(cl), n_rows, len(cl), n_roots, C.byref(h))
+        else:
+            rp = np.ascontiguousarray(row_ptr, np.int32)
+            cl = np.ascontiguousarray(col, np.int32)
+            N.call("tc_graph_upload_i32", self._h, _ptr(rp), _ptr(cl), n_rows, len(cl), n_roots, C.byref(h))
+        return Graph(self, h)
+
+    def count(self, g: Graph, stats: bool = False):
+        out = C.c_uint64()
+        st = N.CountStats()
+        N.call("tc_count", self._h, g.handle, C.byref(out), C.byref(st))
+        if stats:
+            return out.value, {"count_ms": st.count_ms, "finalize_ms": st.finalize_ms,
+                               "launches": st.launches, "heavy_units": st.heavy_units}
+        return out.value
+
+    def count_per_root(self, g: Graph) -> np.ndarray:
+        out = np.empty(max(g.n_roots, 0), np.uint64)
+        tot = C.c_uint64()
+        N.call("tc_count_per_root", self._h, g.handle, _ptr(out), C.byref(tot))
+        return out
+
+    def count_csr(self, row_ptr: np.ndarray, col: np.ndarray) -> int:
+        """End to end from host arrays: upload, validate, count, read back."""
+        rp = np.ascontiguousarray(row_ptr, np.int32)
+        cl = np.ascontiguousarray(col, np.int32)
+        out = C.c_uint64()
+        N.call("tc_count_csr_i32", self._h, _ptr(rp), _ptr(cl), len(rp) - 1, len(cl), C.byref(out))
+        return out.value
+
+    def count_each(self, graphs: Sequence[Graph]) -> np.ndarray:
+        arr = (C.c_void_p * len(graphs))(*[g.handle for g in graphs])
+        out = np.empty(len(graphs), np.uint64)
+        N.call("tc_count_each", self._h, arr, len(graphs), _ptr(out))
+        return out
+
+    def batch(self, graphs: Sequence[Graph]) -> Batch:
+        return Batch(self, graphs)
+
+    # ---- preprocessing ----
+    def ugraph_from_edges(self, src: np.ndarray, dst: np.ndarray, n_nodes: int = 0) -> UGraph:
+        s = np.ascontiguousarray(src, np.int64)
+        d = np.ascontiguousarray(dst, np.int64)
+        h = C.c_void_p()
+        N.call("tc_ugraph_from_edges", self._h, _ptr(s), _ptr(d), len(s), int(n_nodes), C.byref(h))
+        return UGraph(self, h)
+
+    def upload_ugraph(self, row_ptr: np.ndarray, col: np.ndarray, deg: np.ndarray | None = None) -> UGraph:
+        rp = np.ascontiguousarray(row_ptr, np.int64)
+        cl = np.ascontiguousarray(col, np.int64)
+        dg = None if deg is None else np.ascontiguousarray(deg, np.int64)
+        h = C.c_void_p()
+        N.call("tc_ugraph_upload_i64", self._h, _ptr(rp), _ptr(cl), _ptr(dg), len(rp) - 1, len(cl), C.byref(h))
+        return UGraph(self, h)
+
+    def orient(self, ug: UGraph, tie="reference") -> Graph:
+        h = C.c_void_p()
+        N.call("tc_orient", self._h, ug.handle, _tie(tie), C.byref(h))
+        return Graph(self, h)
+
+    def graph_from_edges(self, src: np.ndarray, dst: np.ndarray, n_nodes: int = 0, tie="reference") -> Graph:
+        s = np.ascontiguousarray(src, np.int64)
+        d = np.ascontiguousarray(dst, np.int64)
+        h = C.c_void_p()
+        N.call("tc_graph_from_edges", self._h, _ptr(s), _ptr(d), len(s), int(n_nodes), _tie(tie), C.byref(h))
+        return Graph(self, h)
+
+    def halo_extract(self, ug: UGraph, part: np.ndarray, k: int, tie="reference") -> list[Graph]:
+        p = np.ascontiguousarray(part, np.int32)
+        outs = (C.c_void_p * k)()
+        N.call("tc_halo_extract", self._h, ug.handle, _ptr(p), int(k), _tie(tie), outs)
+        return [Graph(self, C.c_void_p(outs[i])) for i in range(k)]

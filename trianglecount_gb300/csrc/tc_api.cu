@@ -1,0 +1,637 @@
+// tc_api.cu -- C ABI: contexts, oriented graphs, plain and batched counting.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "tc_internal.h"
+
+namespace tc {
+
+namespace {
+thread_local std::string g_last_error;
+
+constexpr int kVersion = 10000;  // 1.0.0
+
+// ---- CSR validation (rows strictly ascending, ids in range) ----
+struct ValidateErr {
+    int code;     // 0 ok, 1 row_ptr, 2 id range, 3 order
+    int first;    // smallest offending row / entry index
+};
+
+__global__ void mark_rows_kernel(const int32_t *rp, int64_t n_rows, int64_t nnz, uint8_t *start, ValidateErr *err) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n_rows; u += stride) {
+        const int64_t a = rp[u], b = rp[u + 1];
+        const bool bad = a > b || a < 0 || b > nnz || (u == 0 && a != 0) || (u == n_rows - 1 && b != nnz);
+        if (bad) {
+            atomicMax(&err->code, 1);
+            atomicMin(&err->first, (int)u);
+        } else if (a < b) {
+            start[a] = 1;
+        }
+    }
+}
+
+__global__ void check_cols_kernel(const int32_t *col, int64_t nnz, int64_t n_rows, const uint8_t *start,
+                                  ValidateErr *err) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nnz; j += stride) {
+        const int x = col[j];
+        int code = 0;
+        if (x < 0 || x >= n_rows) code = 2;
+        else if (j + 1 < nnz && !start[j + 1] && col[j + 1] <= x) code = 3;
+        if (code) {
+            atomicMax(&err->code, code);
+            atomicMin(&err->first, (int)j);
+        }
+    }
+}
+
+__global__ void narrow_u64_kernel(const uint64_t *in, int32_t *out, int64_t n, uint64_t limit, int *overflow) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint64_t v = in[i];
+        if (v > limit) *overflow = 1;
+        out[i] = (int32_t)v;
+    }
+}
+
+int grid_for(int64_t n, int sm) {
+    const int64_t b = (n + 255) / 256;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)sm * 32));
+}
+
+int validate_csr_impl(tc_ctx *ctx, const int32_t *rp, const int32_t *col, int64_t n_rows, int64_t nnz) {
+    cudaStream_t s = ctx->stream;
+    DBuf<uint8_t> start;
+    DBuf<ValidateErr> err;
+    TC_TRY(start.alloc((size_t)nnz + 1, s));
+    TC_TRY(err.alloc(1, s));
+    TC_CUDA(cudaMemsetAsync(start.p, 0, (size_t)nnz + 1, s));
+    ValidateErr init{0, 0x7fffffff};
+    TC_CUDA(cudaMemcpyAsync(err.p, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+    if (n_rows > 0) {
+        mark_rows_kernel<<<grid_for(n_rows, ctx->sm_count), 256, 0, s>>>(rp, n_rows, nnz, start.p, err.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    if (nnz > 0) {
+        check_cols_kernel<<<grid_for(nnz, ctx->sm_count), 256, 0, s>>>(col, nnz, n_rows, start.p, err.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    ValidateErr h;
+    TC_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+    TC_CUDA(cudaStreamSynchronize(s));
+    if (n_rows == 0 && nnz != 0) return set_error(TC_E_FORMAT, "CSR has 0 rows but %lld entries", (long long)nnz);
+    switch (h.code) {
+    case 1: return set_error(TC_E_FORMAT, "row_ptr is not a valid offset array at row %d", h.first);
+    case 2: return set_error(TC_E_FORMAT, "column id out of range [0, %lld) at entry %d", (long long)n_rows, h.first);
+    case 3: return set_error(TC_E_FORMAT, "row not strictly ascending at entry %d", h.first);
+    default: return TC_OK;
+    }
+}
+
+int check_graph(const tc_graph *g) {
+    if (!g || !g->ctx) return set_error(TC_E_INVALID, "null graph");
+    return TC_OK;
+}
+
+// Count scratch of a graph: descriptor, work words + result, heavy list.
+int ensure_count_scratch(tc_graph *g) {
+    tc_ctx *ctx = g->ctx;
+    const int64_t cap = g->nnz / (ctx->tuned.warp_max + 1) + 1;
+    if (!g->d_work) {
+        void *p = nullptr;
+        TC_TRY(dalloc(&p, sizeof(CountWork) + sizeof(unsigned long long), ctx->stream));
+        g->d_work = (CountWork *)p;
+        g->d_result = (unsigned long long *)(g->d_work + 1);
+        TC_TRY(dalloc((void **)&g->d_desc, sizeof(GraphDesc), ctx->stream));
+    }
+    if (g->heavy_cap < cap) {
+        if (g->d_heavy) dfree(g->d_heavy, ctx->stream);
+        g->d_heavy = nullptr;
+        TC_TRY(dalloc((void **)&g->d_heavy, sizeof(HeavyEntry) * (size_t)cap, ctx->stream));
+        g->heavy_cap = cap;
+    }
+    return TC_OK;
+}
+
+int enqueue_graph_count(tc_graph *g, unsigned long long *per_root, unsigned long long *results, int *launches) {
+    tc_ctx *ctx = g->ctx;
+    TC_TRY(ensure_count_scratch(g));
+    GraphDesc d;
+    d.rp = g->rp;
+    d.col = g->col;
+    d.n_roots = g->n_roots;
+    d.chunk_base = 0;
+    d.per_root = per_root;
+    TC_CUDA(cudaMemcpyAsync(g->d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, ctx->stream));
+    const int64_t chunks = (g->n_roots + 31) / 32;
+    return launch_count(g->d_desc, 1, chunks, g->d_heavy, g->heavy_cap, g->d_work, results ? results : g->d_result,
+                        ctx->tuned, ctx->stream, launches);
+}
+
+int new_graph(tc_ctx *ctx, int64_t n_rows, int64_t nnz, int64_t n_roots, tc_graph **out) {
+    if (!ctx || !out) return set_error(TC_E_INVALID, "null context or output");
+    if (n_rows < 0 || nnz < 0 || n_roots < 0 || n_roots > n_rows)
+        return set_error(TC_E_INVALID, "bad sizes: n_rows=%lld nnz=%lld n_roots=%lld", (long long)n_rows,
+                         (long long)nnz, (long long)n_roots);
+    if (n_rows >= INT32_MAX || nnz >= INT32_MAX)
+        return set_error(TC_E_RANGE, "graph too large for int32 indices: n_rows=%lld nnz=%lld", (long long)n_rows,
+                         (long long)nnz);
+    tc_graph *g = new tc_graph();
+    g->ctx = ctx;
+    g->n_rows = n_rows;
+    g->nnz = nnz;
+    g->n_roots = n_roots;
+    *out = g;
+    return TC_OK;
+}
+
+}  // namespace
+
+int validate_csr(tc_ctx *ctx, const int32_t *rp, const int32_t *col, int64_t n_rows, int64_t nnz) {
+    return validate_csr_impl(ctx, rp, col, n_rows, nnz);
+}
+
+int set_error(int status, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+int cuda_error(cudaError_t e, const char *what, const char *file, int line) {
+    const char *base = strrchr(file, '/');
+    set_error(e == cudaErrorMemoryAllocation ? TC_E_NOMEM : TC_E_CUDA, "%s failed: %s (%s:%d)", what,
+              cudaGetErrorString(e), base ? base + 1 : file, line);
+    return e == cudaErrorMemoryAllocation ? TC_E_NOMEM : TC_E_CUDA;
+}
+
+int dalloc(void **p, size_t bytes, cudaStream_t s) {
+    cudaError_t e = cudaMallocAsync(p, bytes, s);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_error(e, "cudaMallocAsync", __FILE__, __LINE__);
+    }
+    return TC_OK;
+}
+
+void dfree(void *p, cudaStream_t s) {
+    if (p) cudaFreeAsync(p, s);
+}
+
+int device_sm_count(int device) {
+    int sm = 0;
+    cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
+    return sm;
+}
+
+int graph_adopt_device(tc_ctx *ctx, int32_t *rp, int32_t *col, int64_t n_rows, int64_t nnz, int64_t n_roots,
+                       tc_graph **out) {
+    tc_graph *g = nullptr;
+    TC_TRY(new_graph(ctx, n_rows, nnz, n_roots, &g));
+    g->rp = rp;
+    g->col = col;
+    g->owns = true;
+    *out = g;
+    return TC_OK;
+}
+
+}  // namespace tc
+
+using namespace tc;
+
+// ============================== C ABI ===========================================
+extern "C" {
+
+const char *tc_last_error(void) { return g_last_error.c_str(); }
+
+const char *tc_status_string(int s) {
+    switch (s) {
+    case TC_OK: return "ok";
+    case TC_E_INVALID: return "invalid argument";
+    case TC_E_CUDA: return "CUDA error";
+    case TC_E_NOMEM: return "out of memory";
+    case TC_E_RANGE: return "value out of range";
+    case TC_E_FORMAT: return "malformed input";
+    case TC_E_IO: return "I/O error";
+    case TC_E_NOT_READY: return "not ready";
+    case TC_E_TIMEOUT: return "timed out";
+    case TC_E_NO_DEVICE: return "no CUDA device";
+    case TC_E_STATE: return "wrong state";
+    default: return "unknown status";
+    }
+}
+
+int tc_version(void) { return kVersion; }
+
+int tc_host_alloc_pinned(size_t bytes, void **out) {
+    if (!out) return set_error(TC_E_INVALID, "null output");
+    *out = nullptr;
+    TC_CUDA(cudaMallocHost(out, bytes ? bytes : 1));
+    return TC_OK;
+}
+
+int tc_host_free_pinned(void *p) {
+    if (p) TC_CUDA(cudaFreeHost(p));
+    return TC_OK;
+}
+
+int tc_ctx_create(int device, tc_ctx **out) {
+    if (!out) return set_error(TC_E_INVALID, "null output");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return set_error(TC_E_NO_DEVICE, "no CUDA device available");
+    if (device < 0 || device >= n) return set_error(TC_E_NO_DEVICE, "device %d out of range [0, %d)", device, n);
+    TC_CUDA(cudaSetDevice(device));
+    cudaMemPool_t pool;
+    TC_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t thr = UINT64_MAX;
+    TC_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    tc_ctx *c = new tc_ctx();
+    c->device = device;
+    c->sm_count = device_sm_count(device);
+    c->tuning.warp_max_deg = 128;
+    c->tuning.block_slice = 512;
+    c->tuning.tiny_max_deg = 8;
+    c->tuning.blocks_per_sm = 0;
+    int st = TC_OK;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) st = TC_E_CUDA;
+    c->own_stream = true;
+    for (int i = 0; i < 4 && st == TC_OK; ++i)
+        if (cudaEventCreate(&c->ev[i]) != cudaSuccess) st = TC_E_CUDA;
+    if (st == TC_OK && cudaMallocHost(&c->h_pinned, 4096) != cudaSuccess) st = TC_E_CUDA;
+    if (st == TC_OK) st = resolve_tuning(c->tuning, c->sm_count, &c->tuned);
+    if (st != TC_OK) {
+        if (st == TC_E_CUDA) set_error(st, "context creation failed on device %d", device);
+        tc_ctx_destroy(c);
+        return st;
+    }
+    *out = c;
+    return TC_OK;
+}
+
+int tc_ctx_destroy(tc_ctx *c) {
+    if (!c) return TC_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return TC_OK;
+}
+
+int tc_ctx_set_stream(tc_ctx *c, void *stream) {
+    if (!c) return set_error(TC_E_INVALID, "null context");
+    TC_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    c->stream = (cudaStream_t)stream;
+    c->own_stream = false;
+    return TC_OK;
+}
+
+void *tc_ctx_get_stream(tc_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int tc_ctx_synchronize(tc_ctx *c) {
+    if (!c) return set_error(TC_E_INVALID, "null context");
+    TC_CUDA(cudaStreamSynchronize(c->stream));
+    return TC_OK;
+}
+
+int tc_ctx_device_info(tc_ctx *c, int *sm_count, size_t *free_bytes, size_t *total_bytes) {
+    if (!c) return set_error(TC_E_INVALID, "null context");
+    TC_CUDA(cudaSetDevice(c->device));
+    size_t f = 0, t = 0;
+    TC_CUDA(cudaMemGetInfo(&f, &t));
+    if (sm_count) *sm_count = c->sm_count;
+    if (free_bytes) *free_bytes = f;
+    if (total_bytes) *total_bytes = t;
+    return TC_OK;
+}
+
+int tc_ctx_get_tuning(tc_ctx *c, tc_tuning *out) {
+    if (!c || !out) return set_error(TC_E_INVALID, "null argument");
+    *out = c->tuning;
+    out->blocks_per_sm = c->tuned.blocks / std::max(1, c->sm_count);
+    return TC_OK;
+}
+
+int tc_ctx_set_tuning(tc_ctx *c, const tc_tuning *in) {
+    if (!c || !in) return set_error(TC_E_INVALID, "null argument");
+    tc_tuning t = c->tuning;
+    if (in->warp_max_deg > 0) t.warp_max_deg = in->warp_max_deg;
+    if (in->block_slice > 0) t.block_slice = in->block_slice;
+    if (in->tiny_max_deg >= 0) t.tiny_max_deg = in->tiny_max_deg;
+    if (in->blocks_per_sm >= 0) t.blocks_per_sm = in->blocks_per_sm;
+    Tuned r;
+    TC_TRY(resolve_tuning(t, c->sm_count, &r));
+    c->tuning = t;
+    c->tuned = r;
+    return TC_OK;
+}
+
+int tc_graph_upload_i32(tc_ctx *ctx, const int32_t *row_ptr, const int32_t *col, int64_t n_rows, int64_t nnz,
+                        int64_t n_roots, tc_graph **out) {
+    if (!ctx || !row_ptr || (nnz > 0 && !col) || !out) return set_error(TC_E_INVALID, "null argument");
+    *out = nullptr;
+    tc_graph *g = nullptr;
+    TC_TRY(new_graph(ctx, n_rows, nnz, n_roots, &g));
+    cudaStream_t s = ctx->stream;
+    int st = dalloc((void **)&g->rp, sizeof(int32_t) * (size_t)(n_rows + 1), s);
+    if (st == TC_OK) st = dalloc((void **)&g->col, sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1), s);
+    if (st == TC_OK && cudaMemcpyAsync(g->rp, row_ptr, sizeof(int32_t) * (size_t)(n_rows + 1), cudaMemcpyHostToDevice,
+                                       s) != cudaSuccess)
+        st = set_error(TC_E_CUDA, "row_ptr upload failed");
+    if (st == TC_OK && nnz > 0 &&
+        cudaMemcpyAsync(g->col, col, sizeof(int32_t) * (size_t)nnz, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        st = set_error(TC_E_CUDA, "col upload failed");
+    if (st == TC_OK) st = validate_csr_impl(ctx, g->rp, g->col, n_rows, nnz);
+    if (st != TC_OK) {
+        tc_graph_destroy(g);
+        return st;
+    }
+    *out = g;
+    return TC_OK;
+}
+
+int tc_graph_upload_u64(tc_ctx *ctx, const uint64_t *row_ptr, const uint64_t *col, int64_t n_rows, int64_t nnz,
+                        int64_t n_roots, tc_graph **out) {
+    if (!ctx || !row_ptr || (nnz > 0 && !col) || !out) return set_error(TC_E_INVALID, "null argument");
+    *out = nullptr;
+    tc_graph *g = nullptr;
+    TC_TRY(new_graph(ctx, n_rows, nnz, n_roots, &g));
+    cudaStream_t s = ctx->stream;
+    DBuf<uint64_t> stage;
+    DBuf<int> ovf;
+    int st = dalloc((void **)&g->rp, sizeof(int32_t) * (size_t)(n_rows + 1), s);
+    if (st == TC_OK) st = dalloc((void **)&g->col, sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1), s);
+    if (st == TC_OK) st = stage.alloc((size_t)std::max(n_rows + 1, nnz), s);
+    if (st == TC_OK) st = ovf.alloc(1, s);
+    if (st == TC_OK && cudaMemsetAsync(ovf.p, 0, sizeof(int), s) != cudaSuccess) st = TC_E_CUDA;
+    const uint64_t *srcs[2] = {row_ptr, col};
+    int32_t *dsts[2] = {g->rp, g->col};
+    const int64_t ns[2] = {n_rows + 1, nnz};
+    for (int k = 0; k < 2 && st == TC_OK; ++k) {
+        if (ns[k] == 0) continue;
+        if (cudaMemcpyAsync(stage.p, srcs[k], sizeof(uint64_t) * (size_t)ns[k], cudaMemcpyHostToDevice, s) !=
+            cudaSuccess) {
+            st = set_error(TC_E_CUDA, "u64 upload failed");
+            break;
+        }
+        narrow_u64_kernel<<<grid_for(ns[k], ctx->sm_count), 256, 0, s>>>(stage.p, dsts[k], ns[k], INT32_MAX - 1,
+                                                                          ovf.p);
+        if (cudaGetLastError() != cudaSuccess) st = set_error(TC_E_CUDA, "narrow kernel launch failed");
+    }
+    int h_ovf = 0;
+    if (st == TC_OK && (cudaMemcpyAsync(&h_ovf, ovf.p, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                        cudaStreamSynchronize(s) != cudaSuccess))
+        st = set_error(TC_E_CUDA, "u64 narrowing failed");
+    if (st == TC_OK && h_ovf) st = set_error(TC_E_RANGE, "u64 CSR value does not fit int32");
+    if (st == TC_OK) st = validate_csr_impl(ctx, g->rp, g->col, n_rows, nnz);
+    if (st != TC_OK) {
+        tc_graph_destroy(g);
+        return st;
+    }
+    *out = g;
+    return TC_OK;
+}
+
+int tc_graph_wrap_device_i32(tc_ctx *ctx, const int32_t *d_row_ptr, const int32_t *d_col, int64_t n_rows, int64_t nnz,
+                             int64_t n_roots, tc_graph **out) {
+    if (!ctx || !d_row_ptr || !out) return set_error(TC_E_INVALID, "null argument");
+    tc_graph *g = nullptr;
+    TC_TRY(new_graph(ctx, n_rows, nnz, n_roots, &g));
+    g->rp = const_cast<int32_t *>(d_row_ptr);
+    g->col = const_cast<int32_t *>(d_col);
+    g->owns = false;
+    *out = g;
+    return TC_OK;
+}
+
+int tc_graph_info(const tc_graph *g, int64_t *n_rows, int64_t *nnz, int64_t *n_roots) {
+    TC_TRY(check_graph(g));
+    if (n_rows) *n_rows = g->n_rows;
+    if (nnz) *nnz = g->nnz;
+    if (n_roots) *n_roots = g->n_roots;
+    return TC_OK;
+}
+
+int tc_graph_download_i32(tc_ctx *ctx, const tc_graph *g, int32_t *row_ptr, int32_t *col) {
+    TC_TRY(check_graph(g));
+    if (!ctx) ctx = g->ctx;
+    if (row_ptr)
+        TC_CUDA(cudaMemcpyAsync(row_ptr, g->rp, sizeof(int32_t) * (size_t)(g->n_rows + 1), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+    if (col && g->nnz)
+        TC_CUDA(cudaMemcpyAsync(col, g->col, sizeof(int32_t) * (size_t)g->nnz, cudaMemcpyDeviceToHost, ctx->stream));
+    TC_CUDA(cudaStreamSynchronize(ctx->stream));
+    return TC_OK;
+}
+
+int tc_graph_destroy(tc_graph *g) {
+    if (!g) return TC_OK;
+    cudaStream_t s = g->ctx ? g->ctx->stream : nullptr;
+    if (g->owns) {
+        dfree(g->rp, s);
+        dfree(g->col, s);
+    }
+    dfree(g->d_desc, s);
+    dfree(g->d_work, s);
+    dfree(g->d_heavy, s);
+    delete g;
+    return TC_OK;
+}
+
+int tc_count(tc_ctx *ctx, tc_graph *g, uint64_t *out, tc_count_stats *stats) {
+    TC_TRY(check_graph(g));
+    if (!out) return set_error(TC_E_INVALID, "null output");
+    if (!ctx) ctx = g->ctx;
+    if (g->ctx != ctx) return set_error(TC_E_INVALID, "graph belongs to another context");
+    cudaStream_t s = ctx->stream;
+    int launches = 0;
+    TC_CUDA(cudaEventRecord(ctx->ev[0], s));
+    TC_TRY(enqueue_graph_count(g, nullptr, nullptr, &launches));
+    TC_CUDA(cudaEventRecord(ctx->ev[1], s));
+    TC_CUDA(cudaMemcpyAsync(ctx->h_pinned, g->d_work, sizeof(CountWork) + sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, s));
+    TC_CUDA(cudaEventRecord(ctx->ev[2], s));
+    TC_CUDA(cudaStreamSynchronize(s));
+    const CountWork *w = (const CountWork *)ctx->h_pinned;
+    if (w->error) return set_error(TC_E_STATE, "heavy-unit list overflow (tuning changed under a graph?)");
+    *out = *(const unsigned long long *)(w + 1);
+    if (stats) {
+        TC_CUDA(cudaEventElapsedTime(&stats->count_ms, ctx->ev[0], ctx->ev[1]));
+        TC_CUDA(cudaEventElapsedTime(&stats->finalize_ms, ctx->ev[1], ctx->ev[2]));
+        stats->launches = launches;
+        stats->heavy_units = (int32_t)(w->heavy_packed & 0xffffffffull);
+    }
+    return TC_OK;
+}
+
+int tc_count_async(tc_ctx *ctx, tc_graph *g, uint64_t *d_out) {
+    TC_TRY(check_graph(g));
+    if (!d_out) return set_error(TC_E_INVALID, "null output");
+    if (!ctx) ctx = g->ctx;
+    return enqueue_graph_count(g, nullptr, (unsigned long long *)d_out, nullptr);
+}
+
+int tc_count_per_root(tc_ctx *ctx, tc_graph *g, uint64_t *per_root, uint64_t *total) {
+    TC_TRY(check_graph(g));
+    if (!per_root) return set_error(TC_E_INVALID, "null output");
+    if (!ctx) ctx = g->ctx;
+    cudaStream_t s = ctx->stream;
+    DBuf<unsigned long long> pr;
+    TC_TRY(pr.alloc((size_t)std::max<int64_t>(g->n_roots, 1), s));
+    TC_CUDA(cudaMemsetAsync(pr.p, 0, sizeof(unsigned long long) * (size_t)std::max<int64_t>(g->n_roots, 1), s));
+    TC_TRY(enqueue_graph_count(g, pr.p, nullptr, nullptr));
+    if (g->n_roots)
+        TC_CUDA(cudaMemcpyAsync(per_root, pr.p, sizeof(unsigned long long) * (size_t)g->n_roots,
+                                cudaMemcpyDeviceToHost, s));
+    TC_CUDA(cudaMemcpyAsync(ctx->h_pinned, g->d_work, sizeof(CountWork), cudaMemcpyDeviceToHost, s));
+    TC_CUDA(cudaStreamSynchronize(s));
+    if (((const CountWork *)ctx->h_pinned)->error) return set_error(TC_E_STATE, "heavy-unit list overflow");
+    if (total) {
+        uint64_t t = 0;
+        for (int64_t u = 0; u < g->n_roots; ++u) t += per_root[u];
+        *total = t;
+    }
+    return TC_OK;
+}
+
+int tc_count_csr_i32(tc_ctx *ctx, const int32_t *row_ptr, const int32_t *col, int64_t n_rows, int64_t nnz,
+                     uint64_t *out) {
+    tc_graph *g = nullptr;
+    TC_TRY(tc_graph_upload_i32(ctx, row_ptr, col, n_rows, nnz, n_rows, &g));
+    int st = tc_count(ctx, g, out, nullptr);
+    tc_graph_destroy(g);
+    return st;
+}
+
+int tc_count_each(tc_ctx *ctx, tc_graph *const *graphs, int n, uint64_t *outs) {
+    if (!ctx || (n > 0 && (!graphs || !outs))) return set_error(TC_E_INVALID, "null argument");
+    for (int i = 0; i < n; ++i) TC_TRY(tc_count(ctx, graphs[i], outs + i, nullptr));
+    return TC_OK;
+}
+
+}  // extern "C"
+
+// ============================== batches =========================================
+struct tc_batch {
+    tc_ctx *ctx = nullptr;
+    int n = 0;
+    std::vector<tc_graph *> graphs;
+    GraphDesc *d_desc = nullptr;
+    HeavyEntry *d_heavy = nullptr;
+    int64_t heavy_cap = 0;
+    CountWork *d_work = nullptr;  // followed by n results
+    unsigned long long *h_out = nullptr;  // pinned: CountWork + n results
+    int64_t total_chunks = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" {
+
+int tc_batch_destroy(tc_batch *b) {
+    if (!b) return TC_OK;
+    cudaStream_t s = b->ctx ? b->ctx->stream : nullptr;
+    if (s) cudaStreamSynchronize(s);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    dfree(b->d_desc, s);
+    dfree(b->d_heavy, s);
+    dfree(b->d_work, s);
+    if (b->h_out) cudaFreeHost(b->h_out);
+    delete b;
+    return TC_OK;
+}
+
+int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out) {
+    if (!ctx || !out || n <= 0 || !graphs) return set_error(TC_E_INVALID, "bad batch arguments");
+    *out = nullptr;
+    tc_batch *b = new tc_batch();
+    b->ctx = ctx;
+    b->n = n;
+    cudaStream_t s = ctx->stream;
+    std::vector<GraphDesc> desc((size_t)n);
+    int64_t chunks = 0, cap = 0;
+    for (int i = 0; i < n; ++i) {
+        tc_graph *g = graphs[i];
+        if (!g || g->ctx != ctx) {
+            tc_batch_destroy(b);
+            return set_error(TC_E_INVALID, "graph %d is null or belongs to another context", i);
+        }
+        b->graphs.push_back(g);
+        desc[i].rp = g->rp;
+        desc[i].col = g->col;
+        desc[i].n_roots = g->n_roots;
+        desc[i].chunk_base = chunks;
+        desc[i].per_root = nullptr;
+        chunks += (g->n_roots + 31) / 32;
+        cap += g->nnz / (ctx->tuned.warp_max + 1) + 1;
+    }
+    b->total_chunks = chunks;
+    b->heavy_cap = cap;
+    int st = dalloc((void **)&b->d_desc, sizeof(GraphDesc) * (size_t)n, s);
+    if (st == TC_OK) st = dalloc((void **)&b->d_heavy, sizeof(HeavyEntry) * (size_t)cap, s);
+    if (st == TC_OK) st = dalloc((void **)&b->d_work, sizeof(CountWork) + sizeof(unsigned long long) * (size_t)n, s);
+    if (st == TC_OK && cudaMallocHost(&b->h_out, sizeof(CountWork) + sizeof(unsigned long long) * (size_t)n) != cudaSuccess)
+        st = set_error(TC_E_NOMEM, "pinned result buffer");
+    if (st == TC_OK && cudaMemcpyAsync(b->d_desc, desc.data(), sizeof(GraphDesc) * (size_t)n, cudaMemcpyHostToDevice,
+                                       s) != cudaSuccess)
+        st = set_error(TC_E_CUDA, "descriptor upload failed");
+    if (st == TC_OK && cudaStreamSynchronize(s) != cudaSuccess) st = set_error(TC_E_CUDA, "batch setup sync failed");
+    // capture [memset -> classify -> count] once; tc_batch_run replays it
+    if (st == TC_OK && cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        st = set_error(TC_E_CUDA, "stream capture could not start");
+    if (st == TC_OK) {
+        int ls = launch_count(b->d_desc, n, chunks, b->d_heavy, cap, b->d_work,
+                              (unsigned long long *)(b->d_work + 1), ctx->tuned, s, nullptr);
+        cudaError_t e = cudaStreamEndCapture(s, &b->graph);
+        if (ls != TC_OK) st = ls;
+        else if (e != cudaSuccess) st = cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+    }
+    if (st == TC_OK) {
+        cudaError_t e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+        if (e != cudaSuccess) st = cuda_error(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+    }
+    if (st != TC_OK) {
+        tc_batch_destroy(b);
+        return st;
+    }
+    *out = b;
+    return TC_OK;
+}
+
+int tc_batch_run_async(tc_batch *b) {
+    if (!b) return set_error(TC_E_INVALID, "null batch");
+    TC_CUDA(cudaGraphLaunch(b->exec, b->ctx->stream));
+    return TC_OK;
+}
+
+int tc_batch_results(tc_batch *b, uint64_t *outs) {
+    if (!b || !outs) return set_error(TC_E_INVALID, "null argument");
+    cudaStream_t s = b->ctx->stream;
+    TC_CUDA(cudaMemcpyAsync(b->h_out, b->d_work, sizeof(CountWork) + sizeof(unsigned long long) * (size_t)b->n,
+                            cudaMemcpyDeviceToHost, s));
+    TC_CUDA(cudaStreamSynchronize(s));
+    const CountWork *w = (const CountWork *)b->h_out;
+    if (w->error) return set_error(TC_E_STATE, "heavy-unit list overflow");
+    memcpy(outs, (const void *)(w + 1), sizeof(uint64_t) * (size_t)b->n);
+    return TC_OK;
+}
+
+int tc_batch_run(tc_batch *b, uint64_t *outs) {
+    TC_TRY(tc_batch_run_async(b));
+    return tc_batch_results(b, outs);
+}
+
+}  // extern "C"

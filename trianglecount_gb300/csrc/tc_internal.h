@@ -1,0 +1,153 @@
+// tc_internal.h -- shared declarations of libtc's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "tc.h"
+
+namespace tc {
+
+// ---- errors ------------------------------------------------------------------
+// Records a message for tc_last_error() on the calling thread; returns status.
+int set_error(int status, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
+int cuda_error(cudaError_t e, const char *what, const char *file, int line);
+
+#define TC_CUDA(call)                                                                 \
+    do {                                                                              \
+        cudaError_t tc_e_ = (call);                                                   \
+        if (tc_e_ != cudaSuccess) return ::tc::cuda_error(tc_e_, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define TC_TRY(call)                    \
+    do {                                \
+        int tc_s_ = (call);             \
+        if (tc_s_ != TC_OK) return tc_s_; \
+    } while (0)
+
+// ---- device scratch ------------------------------------------------------------
+// Stream-ordered allocation from the device's default memory pool (its release
+// threshold is raised at context creation, so freed blocks stay cached and a
+// steady-state call does not reach the driver allocator).
+int dalloc(void **p, size_t bytes, cudaStream_t s);
+void dfree(void *p, cudaStream_t s);
+
+template <class T>
+struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaStream_t s = nullptr;
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    ~DBuf() { reset(); }
+    int alloc(size_t count, cudaStream_t stream) {
+        reset();
+        s = stream;
+        n = count;
+        return dalloc((void **)&p, (count ? count : 1) * sizeof(T), stream);
+    }
+    void reset() {
+        if (p) dfree(p, s);
+        p = nullptr;
+        n = 0;
+    }
+    T *release() {
+        T *q = p;
+        p = nullptr;
+        n = 0;
+        return q;
+    }
+};
+
+// ---- counting kernels (tc_count.cu) ----------------------------------------------
+struct GraphDesc {
+    const int32_t *rp;
+    const int32_t *col;
+    int64_t n_roots;
+    int64_t chunk_base;           // exclusive prefix of 32-root chunks over graphs
+    unsigned long long *per_root; // optional g_sum output (zeroed by the caller)
+};
+
+struct HeavyEntry {
+    int32_t g, u, unit_base, n_units;
+};
+
+// Per-launch device words, zeroed by one memset before each count.
+struct CountWork {
+    unsigned long long heavy_packed; // (entries << 32) | units, from the classifier
+    unsigned int heavy_cursor;
+    unsigned int small_cursor;
+    int error;
+    int pad;
+};
+
+struct Tuned {  // resolved tc_tuning with derived table geometry
+    int warp_max;      // power of two
+    int log_warp_slots;
+    int slice;
+    int tile;          // block table entries per tile
+    int log_block_slots;
+    int tiny_max;
+    int threads;       // per block
+    int blocks;        // persistent grid
+    size_t smem;       // dynamic shared memory bytes
+};
+
+int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out);
+
+// Enqueues classify + persistent count for n_graphs descriptors on stream s.
+// results[n_graphs] receives the per-graph totals (zeroed here).
+int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, HeavyEntry *heavy, int64_t heavy_cap,
+                 CountWork *work, unsigned long long *results, const Tuned &tn, cudaStream_t s, int *launches);
+
+// ---- scans and sort (tc_scan.cu, tc_sort.cu) ----------------------------------------
+// Exclusive scan of n values into out[0..n] (out[n] = total).  out may alias in.
+int scan_exclusive_i32(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s);
+int scan_exclusive_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s);
+// Exclusive scan of 0/1 byte flags into int32 positions out[0..n].
+int scan_flags_u8(const uint8_t *flags, int32_t *out, int64_t n, cudaStream_t s);
+// LSD radix sort of n 64-bit keys on bits [0, bits).  Result in *keys (the
+// two buffers may be swapped).  tmp must hold n keys.
+int radix_sort_u64(uint64_t **keys, uint64_t **tmp, int64_t n, int bits, cudaStream_t s);
+
+int device_sm_count(int device);
+
+}  // namespace tc
+
+// ---- library object layouts ----------------------------------------------------------
+struct tc_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int sm_count = 0;
+    tc_tuning tuning{};
+    tc::Tuned tuned{};
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    unsigned long long *h_pinned = nullptr;  // small pinned read-back area
+};
+
+struct tc_graph {
+    tc_ctx *ctx = nullptr;
+    int32_t *rp = nullptr;
+    int32_t *col = nullptr;
+    int64_t n_rows = 0, nnz = 0, n_roots = 0;
+    bool owns = true;
+    // per-graph count scratch, sized on first use
+    tc::GraphDesc *d_desc = nullptr;
+    tc::CountWork *d_work = nullptr;
+    unsigned long long *d_result = nullptr;
+    tc::HeavyEntry *d_heavy = nullptr;
+    int64_t heavy_cap = 0;
+};
+
+struct tc_ugraph {
+    tc_ctx *ctx = nullptr;
+    int32_t *rp = nullptr;
+    int32_t *col = nullptr;
+    int32_t *deg = nullptr;    // degree used for orientation
+    int32_t *rowid = nullptr;  // row of each entry (nnz)
+    int64_t n_rows = 0, nnz = 0;
+};

@@ -1,0 +1,667 @@
+// tc_prep.cu -- device preprocessing: edge list -> simple undirected CSR ->
+// degree-oriented CSR, and per-part halo subgraphs.
+//
+// Clean-up restates the DGL pipeline of Med_dataset/without_part_preprocess.py:193-228
+// (remove_self_loop, to_bidirected, remove isolated nodes, adj_tensors('csr')):
+//   keys (u<<B|v) and (v<<B|u) per non-loop edge -> LSD radix sort -> unique
+//   -> per-vertex counts -> order-preserving relabel of non-isolated vertices.
+// Orientation restates Find_size / cp.cumsum / Convert (:19-111, :253-270):
+//   keep flag per entry -> exclusive scan -> stable scatter, so rows stay ascending.
+// Halo extraction restates create_subgraph_with_halo
+// (preprocess_GPU/Halo_cleanned_preprocess/round_clean_subgraph.cu:357-902) with the
+// intended prune loop of Halo_creation_preprocess.py:566-589: halo vertices with
+// zero in-degree are peeled until none is left.
+#include <algorithm>
+#include <vector>
+
+#include "tc_internal.h"
+
+namespace tc {
+
+int validate_csr(tc_ctx *ctx, const int32_t *rp, const int32_t *col, int64_t n_rows, int64_t nnz);
+int graph_adopt_device(tc_ctx *ctx, int32_t *rp, int32_t *col, int64_t n_rows, int64_t nnz, int64_t n_roots,
+                       tc_graph **out);
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr uint64_t kSentinel = ~0ull;
+
+#define GRID_STRIDE(i, n) \
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+
+int grid(int64_t n, const tc_ctx *ctx) {
+    const int64_t b = (n + 255) / 256;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)ctx->sm_count * 32));
+}
+
+__device__ __forceinline__ bool keep_edge(int du, int dw, int u, int w, int tie) {
+    if (du != dw) return du < dw;
+    return tie == TC_TIE_REFERENCE ? (w < u) : (u < w);
+}
+
+// Adds 1 to cnt[key] for a warp of (mostly sorted) keys with one atomic per
+// distinct key in the warp.
+__device__ __forceinline__ void warp_count(int32_t *cnt, int key, bool valid) {
+    const unsigned act = __ballot_sync(kFull, valid);
+    if (!valid) return;
+    const unsigned peers = __match_any_sync(act, key);
+    const int lane = threadIdx.x & 31;
+    if ((peers & ((1u << lane) - 1u)) == 0) atomicAdd(&cnt[key], __popc(peers));
+}
+
+__global__ void max_id_kernel(const int64_t *a, const int64_t *b, int64_t n, unsigned long long *mx, int *neg) {
+    unsigned long long m = 0;
+    bool bad = false;
+    GRID_STRIDE(i, n) {
+        const int64_t x = a[i], y = b[i];
+        bad |= (x < 0) | (y < 0);
+        m = max(m, (unsigned long long)max(x, y));
+    }
+    if (bad) *neg = 1;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) m = max(m, __shfl_xor_sync(kFull, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
+}
+
+__global__ void make_keys_kernel(const int64_t *src, const int64_t *dst, int64_t n, int B, uint64_t *keys) {
+    GRID_STRIDE(i, n) {
+        const uint64_t u = (uint64_t)src[i], v = (uint64_t)dst[i];
+        if (u == v) {
+            keys[2 * i] = kSentinel;
+            keys[2 * i + 1] = kSentinel;
+        } else {
+            keys[2 * i] = (u << B) | v;
+            keys[2 * i + 1] = (v << B) | u;
+        }
+    }
+}
+
+__global__ void unique_flags_kernel(const uint64_t *keys, int64_t n, uint8_t *flags) {
+    GRID_STRIDE(i, n) {
+        const uint64_t k = keys[i];
+        flags[i] = (uint8_t)(k != kSentinel && (i == 0 || keys[i - 1] != k));
+    }
+}
+
+__global__ void unique_scatter_kernel(const uint64_t *keys, int64_t n, const uint8_t *flags, const int32_t *pos, int B,
+                                      int32_t *col, int32_t *rowid, int32_t *cnt) {
+    const uint64_t mask = (1ull << B) - 1ull;
+    // every thread of a warp runs the same number of iterations (warp_count needs them all)
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t start = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t rounds = (n + stride - 1) / stride;
+    for (int64_t r = 0; r < rounds; ++r) {
+        const int64_t i = start + r * stride;
+        const bool f = i < n && flags[i];
+        int u = 0;
+        if (f) {
+            const uint64_t k = keys[i];
+            u = (int)(k >> B);
+            const int32_t p = pos[i];
+            col[p] = (int32_t)(k & mask);
+            rowid[p] = u;
+        }
+        warp_count(cnt, u, f);
+    }
+}
+
+__global__ void keep_nonisolated_kernel(const int32_t *cnt, int64_t n, uint8_t *keep) {
+    GRID_STRIDE(v, n) keep[v] = (uint8_t)(cnt[v] > 0);
+}
+
+__global__ void relabel_rows_kernel(const uint8_t *keep, const int32_t *newid, const int32_t *rs_old, int64_t n0,
+                                    int32_t *rp) {
+    GRID_STRIDE(v, n0) {
+        if (keep[v]) rp[newid[v]] = rs_old[v];
+    }
+}
+
+__global__ void remap_kernel(int32_t *a, int64_t n, const int32_t *map) {
+    GRID_STRIDE(i, n) a[i] = map[a[i]];
+}
+
+__global__ void degree_kernel(const int32_t *rp, int64_t n, int32_t *deg) {
+    GRID_STRIDE(v, n) deg[v] = rp[v + 1] - rp[v];
+}
+
+// rowid[j] = u for j in row u (one warp per row)
+__global__ void rowid_kernel(const int32_t *rp, int64_t n_rows, int32_t *rowid) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = w0; u < n_rows; u += nw)
+        for (int64_t j = rp[u] + lane; j < rp[u + 1]; j += 32) rowid[j] = (int32_t)u;
+}
+
+__global__ void narrow_i64_kernel(const int64_t *in, int32_t *out, int64_t n, int64_t limit, int *bad) {
+    GRID_STRIDE(i, n) {
+        const int64_t v = in[i];
+        if (v < 0 || v > limit) *bad = 1;
+        out[i] = (int32_t)v;
+    }
+}
+
+__global__ void orient_flags_kernel(const int32_t *rowid, const int32_t *col, const int32_t *deg, int64_t nnz, int tie,
+                                    uint8_t *flags) {
+    GRID_STRIDE(j, nnz) {
+        const int u = rowid[j], w = col[j];
+        flags[j] = (uint8_t)keep_edge(deg[u], deg[w], u, w, tie);
+    }
+}
+
+__global__ void compact_i32_kernel(const int32_t *in, const uint8_t *flags, const int32_t *pos, int64_t n,
+                                   int32_t *out) {
+    GRID_STRIDE(j, n) {
+        if (flags[j]) out[pos[j]] = in[j];
+    }
+}
+
+__global__ void gather_rp_kernel(const int32_t *rp, const int32_t *pos, int64_t n_rows_plus1, int32_t *out_rp) {
+    GRID_STRIDE(u, n_rows_plus1) out_rp[u] = pos[rp[u]];
+}
+
+// ---- halo ----------------------------------------------------------------------
+__global__ void part_flags_kernel(const int32_t *part, int64_t n, int p, uint8_t *inP) {
+    GRID_STRIDE(v, n) inP[v] = (uint8_t)(part[v] == p);
+}
+
+__global__ void halo_flags_kernel(const int32_t *rowid, const int32_t *col, int64_t nnz, const int32_t *part, int p,
+                                  uint8_t *inH) {
+    GRID_STRIDE(j, nnz) {
+        const int d = col[j];
+        if (part[rowid[j]] == p && part[d] != p) inH[d] = 1;
+    }
+}
+
+__global__ void local_ids_kernel(const uint8_t *inP, const uint8_t *inH, const int32_t *lidP, const int32_t *lidH,
+                                 int64_t n, int t_ver, int32_t *lid) {
+    GRID_STRIDE(v, n) lid[v] = inP[v] ? lidP[v] : (inH[v] ? t_ver + lidH[v] : -1);
+}
+
+// flagsP/flagsH: entry j of a combined source is an oriented edge to a part
+// (P) or halo (H) vertex of the combined set.  cnt[lid(src)] counts both.
+__global__ void halo_edge_flags_kernel(const int32_t *rowid, const int32_t *col, const int32_t *deg, int64_t nnz,
+                                       const int32_t *lid, const uint8_t *inP, int tie, uint8_t *fP, uint8_t *fH,
+                                       int32_t *cnt) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t start = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t rounds = (nnz + stride - 1) / stride;
+    for (int64_t r = 0; r < rounds; ++r) {
+        const int64_t j = start + r * stride;
+        bool keep = false;
+        int ls = 0;
+        if (j < nnz) {
+            const int s = rowid[j], d = col[j];
+            ls = lid[s];
+            const int ld = lid[d];
+            keep = ls >= 0 && ld >= 0 && keep_edge(deg[s], deg[d], s, d, tie);
+            const bool toP = keep && inP[d];
+            fP[j] = (uint8_t)toP;
+            fH[j] = (uint8_t)(keep && !toP);
+        }
+        warp_count(cnt, ls, keep);
+    }
+}
+
+__global__ void halo_scatter_kernel(const int32_t *rowid, const int32_t *col, const int32_t *rp, int64_t nnz,
+                                    const int32_t *lid, const uint8_t *fP, const uint8_t *fH, const int32_t *posP,
+                                    const int32_t *posH, const int32_t *lrp, int32_t *lcol, int32_t *lrow) {
+    GRID_STRIDE(j, nnz) {
+        if (!fP[j] && !fH[j]) continue;
+        const int s = rowid[j];
+        const int a = rp[s], b = rp[s + 1];
+        const int ls = lid[s];
+        int off;
+        if (fP[j]) off = posP[j] - posP[a];
+        else off = (posP[b] - posP[a]) + (posH[j] - posH[a]);
+        const int o = lrp[ls] + off;
+        lcol[o] = lid[col[j]];
+        lrow[o] = ls;
+    }
+}
+
+__global__ void indeg_kernel(const int32_t *lcol, int64_t n, int32_t *indeg) {
+    GRID_STRIDE(j, n) atomicAdd(&indeg[lcol[j]], 1);
+}
+
+__global__ void frontier_init_kernel(const int32_t *indeg, int64_t n, int t_ver, uint8_t *removed, int32_t *front,
+                                     int32_t *front_n) {
+    GRID_STRIDE(i, n) {
+        if (i >= t_ver && indeg[i] == 0) {
+            removed[i] = 1;
+            front[atomicAdd(front_n, 1)] = (int32_t)i;
+        }
+    }
+}
+
+// one warp per frontier vertex: drop its out-edges; halo targets reaching
+// in-degree 0 join the next frontier (exactly once: the 1 -> 0 transition).
+__global__ void peel_kernel(const int32_t *front, int n_front, const int32_t *lrp, const int32_t *lcol, int t_ver,
+                            int32_t *indeg, uint8_t *removed, int32_t *next, int32_t *next_n) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t f = w0; f < n_front; f += nw) {
+        const int x = front[f];
+        for (int j = lrp[x] + lane; j < lrp[x + 1]; j += 32) {
+            const int d = lcol[j];
+            if (atomicSub(&indeg[d], 1) == 1 && d >= t_ver) {
+                removed[d] = 1;
+                next[atomicAdd(next_n, 1)] = d;
+            }
+        }
+    }
+}
+
+__global__ void alive_kernel(const uint8_t *removed, const int32_t *lrp, int64_t n, uint8_t *alive, int32_t *len) {
+    GRID_STRIDE(i, n) {
+        const bool a = !removed[i];
+        alive[i] = (uint8_t)a;
+        len[i] = a ? lrp[i + 1] - lrp[i] : 0;
+    }
+}
+
+__global__ void prune_rows_kernel(const uint8_t *alive, const int32_t *nid, const int32_t *newpos, int64_t n,
+                                  int32_t *rp2) {
+    GRID_STRIDE(i, n) {
+        if (alive[i]) rp2[nid[i]] = newpos[i];
+    }
+}
+
+__global__ void prune_cols_kernel(const int32_t *lrow, const int32_t *lcol, const int32_t *lrp, int64_t nnz,
+                                  const uint8_t *alive, const int32_t *nid, const int32_t *newpos, int32_t *col2) {
+    GRID_STRIDE(e, nnz) {
+        const int i = lrow[e];
+        if (alive[i]) col2[newpos[i] + (int)(e - lrp[i])] = nid[lcol[e]];
+    }
+}
+
+template <class T>
+int d2h_scalar(T *h, const T *d, cudaStream_t s) {
+    TC_CUDA(cudaMemcpyAsync(h, d, sizeof(T), cudaMemcpyDeviceToHost, s));
+    TC_CUDA(cudaStreamSynchronize(s));
+    return TC_OK;
+}
+
+int finish_ugraph(tc_ctx *ctx, int32_t *rp, int32_t *col, int32_t *deg, int32_t *rowid, int64_t n_rows, int64_t nnz,
+                  tc_ugraph **out) {
+    tc_ugraph *g = new tc_ugraph();
+    g->ctx = ctx;
+    g->rp = rp;
+    g->col = col;
+    g->deg = deg;
+    g->rowid = rowid;
+    g->n_rows = n_rows;
+    g->nnz = nnz;
+    *out = g;
+    return TC_OK;
+}
+
+}  // namespace
+
+}  // namespace tc
+
+using namespace tc;
+
+extern "C" {
+
+int tc_ugraph_from_edges(tc_ctx *ctx, const int64_t *src, const int64_t *dst, int64_t n_edges, int64_t n_nodes,
+                         tc_ugraph **out) {
+    if (!ctx || !out || n_edges < 0 || (n_edges > 0 && (!src || !dst)))
+        return set_error(TC_E_INVALID, "bad edge-list arguments");
+    *out = nullptr;
+    if (2 * n_edges >= INT32_MAX) return set_error(TC_E_RANGE, "%lld edges exceed the int32 entry limit", (long long)n_edges);
+    cudaStream_t s = ctx->stream;
+    DBuf<int64_t> dsrc, ddst;
+    DBuf<unsigned long long> dmax;
+    DBuf<int> dneg;
+    TC_TRY(dsrc.alloc((size_t)n_edges, s));
+    TC_TRY(ddst.alloc((size_t)n_edges, s));
+    TC_TRY(dmax.alloc(1, s));
+    TC_TRY(dneg.alloc(1, s));
+    TC_CUDA(cudaMemsetAsync(dmax.p, 0, sizeof(unsigned long long), s));
+    TC_CUDA(cudaMemsetAsync(dneg.p, 0, sizeof(int), s));
+    if (n_edges) {
+        TC_CUDA(cudaMemcpyAsync(dsrc.p, src, sizeof(int64_t) * (size_t)n_edges, cudaMemcpyHostToDevice, s));
+        TC_CUDA(cudaMemcpyAsync(ddst.p, dst, sizeof(int64_t) * (size_t)n_edges, cudaMemcpyHostToDevice, s));
+        max_id_kernel<<<grid(n_edges, ctx), 256, 0, s>>>(dsrc.p, ddst.p, n_edges, dmax.p, dneg.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    unsigned long long mx = 0;
+    int neg = 0;
+    TC_TRY(d2h_scalar(&mx, dmax.p, s));
+    TC_TRY(d2h_scalar(&neg, dneg.p, s));
+    if (neg) return set_error(TC_E_RANGE, "negative vertex id in edge list");
+    const int64_t n0 = std::max<int64_t>(n_nodes, n_edges ? (int64_t)mx + 1 : 0);
+    if (n0 >= INT32_MAX) return set_error(TC_E_RANGE, "vertex id %lld does not fit int32", (long long)n0 - 1);
+    int B = 1;
+    while (B < 31 && ((int64_t)1 << B) < n0) ++B;
+    const int64_t n2 = 2 * n_edges;
+    DBuf<uint64_t> ka, kb;
+    TC_TRY(ka.alloc((size_t)n2, s));
+    TC_TRY(kb.alloc((size_t)n2, s));
+    if (n_edges) {
+        make_keys_kernel<<<grid(n_edges, ctx), 256, 0, s>>>(dsrc.p, ddst.p, n_edges, B, ka.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    dsrc.reset();
+    ddst.reset();
+    uint64_t *keys = ka.p, *tmp = kb.p;
+    TC_TRY(radix_sort_u64(&keys, &tmp, n2, 2 * B, s));
+    DBuf<uint8_t> flags;
+    DBuf<int32_t> pos;
+    TC_TRY(flags.alloc((size_t)n2, s));
+    TC_TRY(pos.alloc((size_t)n2 + 1, s));
+    if (n2) {
+        unique_flags_kernel<<<grid(n2, ctx), 256, 0, s>>>(keys, n2, flags.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    TC_TRY(scan_flags_u8(flags.p, pos.p, n2, s));
+    int32_t nnz32 = 0;
+    TC_TRY(d2h_scalar(&nnz32, pos.p + n2, s));
+    const int64_t nnz = nnz32;
+    DBuf<int32_t> col, rowid, cnt;
+    TC_TRY(col.alloc((size_t)nnz, s));
+    TC_TRY(rowid.alloc((size_t)nnz, s));
+    TC_TRY(cnt.alloc((size_t)n0 + 1, s));
+    TC_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * ((size_t)n0 + 1), s));
+    if (n2) {
+        unique_scatter_kernel<<<grid(n2, ctx), 256, 0, s>>>(keys, n2, flags.p, pos.p, B, col.p, rowid.p, cnt.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    ka.reset();
+    kb.reset();
+    pos.reset();
+    // order-preserving relabel of the non-isolated vertices
+    DBuf<uint8_t> keep;
+    DBuf<int32_t> newid, rs_old;
+    TC_TRY(keep.alloc((size_t)n0, s));
+    TC_TRY(newid.alloc((size_t)n0 + 1, s));
+    TC_TRY(rs_old.alloc((size_t)n0 + 1, s));
+    if (n0) {
+        keep_nonisolated_kernel<<<grid(n0, ctx), 256, 0, s>>>(cnt.p, n0, keep.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    TC_TRY(scan_flags_u8(keep.p, newid.p, n0, s));
+    TC_TRY(scan_exclusive_i32(cnt.p, rs_old.p, n0, s));
+    int32_t V32 = 0;
+    TC_TRY(d2h_scalar(&V32, newid.p + n0, s));
+    const int64_t V = V32;
+    DBuf<int32_t> rp, deg;
+    TC_TRY(rp.alloc((size_t)V + 1, s));
+    TC_TRY(deg.alloc((size_t)std::max<int64_t>(V, 1), s));
+    if (n0) {
+        relabel_rows_kernel<<<grid(n0, ctx), 256, 0, s>>>(keep.p, newid.p, rs_old.p, n0, rp.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    TC_CUDA(cudaMemcpyAsync(rp.p + V, &nnz32, sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    if (nnz) {
+        remap_kernel<<<grid(nnz, ctx), 256, 0, s>>>(col.p, nnz, newid.p);
+        remap_kernel<<<grid(nnz, ctx), 256, 0, s>>>(rowid.p, nnz, newid.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    if (V) {
+        degree_kernel<<<grid(V, ctx), 256, 0, s>>>(rp.p, V, deg.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    TC_CUDA(cudaStreamSynchronize(s));
+    return finish_ugraph(ctx, rp.release(), col.release(), deg.release(), rowid.release(), V, nnz, out);
+}
+
+int tc_ugraph_upload_i64(tc_ctx *ctx, const int64_t *row_ptr, const int64_t *col, const int64_t *deg, int64_t n_rows,
+                         int64_t nnz, tc_ugraph **out) {
+    if (!ctx || !out || !row_ptr || n_rows < 0 || nnz < 0 || (nnz > 0 && !col))
+        return set_error(TC_E_INVALID, "bad undirected CSR arguments");
+    *out = nullptr;
+    if (n_rows >= INT32_MAX || nnz >= INT32_MAX)
+        return set_error(TC_E_RANGE, "undirected CSR too large for int32 indices");
+    cudaStream_t s = ctx->stream;
+    DBuf<int64_t> stage;
+    DBuf<int> bad;
+    DBuf<int32_t> rp, cl, dg, rowid;
+    TC_TRY(stage.alloc((size_t)std::max(n_rows + 1, nnz), s));
+    TC_TRY(bad.alloc(1, s));
+    TC_TRY(rp.alloc((size_t)n_rows + 1, s));
+    TC_TRY(cl.alloc((size_t)nnz, s));
+    TC_TRY(dg.alloc((size_t)std::max<int64_t>(n_rows, 1), s));
+    TC_TRY(rowid.alloc((size_t)nnz, s));
+    TC_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
+    const int64_t *srcs[3] = {row_ptr, col, deg};
+    int32_t *dsts[3] = {rp.p, cl.p, dg.p};
+    const int64_t ns[3] = {n_rows + 1, nnz, deg ? n_rows : 0};
+    for (int k = 0; k < 3; ++k) {
+        if (ns[k] == 0) continue;
+        TC_CUDA(cudaMemcpyAsync(stage.p, srcs[k], sizeof(int64_t) * (size_t)ns[k], cudaMemcpyHostToDevice, s));
+        narrow_i64_kernel<<<grid(ns[k], ctx), 256, 0, s>>>(stage.p, dsts[k], ns[k], INT32_MAX - 1, bad.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    int hbad = 0;
+    TC_TRY(d2h_scalar(&hbad, bad.p, s));
+    if (hbad) return set_error(TC_E_RANGE, "undirected CSR value is negative or does not fit int32");
+    stage.reset();
+    TC_TRY(validate_csr(ctx, rp.p, cl.p, n_rows, nnz));
+    if (!deg && n_rows) {
+        degree_kernel<<<grid(n_rows, ctx), 256, 0, s>>>(rp.p, n_rows, dg.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    if (n_rows) {
+        rowid_kernel<<<grid(n_rows * 32, ctx), 256, 0, s>>>(rp.p, n_rows, rowid.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    TC_CUDA(cudaStreamSynchronize(s));
+    return finish_ugraph(ctx, rp.release(), cl.release(), dg.release(), rowid.release(), n_rows, nnz, out);
+}
+
+int tc_ugraph_info(const tc_ugraph *g, int64_t *n_rows, int64_t *nnz) {
+    if (!g) return set_error(TC_E_INVALID, "null graph");
+    if (n_rows) *n_rows = g->n_rows;
+    if (nnz) *nnz = g->nnz;
+    return TC_OK;
+}
+
+int tc_ugraph_download(tc_ctx *ctx, const tc_ugraph *g, int64_t *row_ptr, int64_t *col, int64_t *deg) {
+    if (!g) return set_error(TC_E_INVALID, "null graph");
+    if (!ctx) ctx = g->ctx;
+    cudaStream_t s = ctx->stream;
+    std::vector<int32_t> tmp;
+    const int32_t *srcs[3] = {g->rp, g->col, g->deg};
+    int64_t *dsts[3] = {row_ptr, col, deg};
+    const int64_t ns[3] = {g->n_rows + 1, g->nnz, g->n_rows};
+    for (int k = 0; k < 3; ++k) {
+        if (!dsts[k] || ns[k] == 0) continue;
+        tmp.resize((size_t)ns[k]);
+        TC_CUDA(cudaMemcpyAsync(tmp.data(), srcs[k], sizeof(int32_t) * (size_t)ns[k], cudaMemcpyDeviceToHost, s));
+        TC_CUDA(cudaStreamSynchronize(s));
+        for (int64_t i = 0; i < ns[k]; ++i) dsts[k][i] = tmp[(size_t)i];
+    }
+    return TC_OK;
+}
+
+int tc_ugraph_destroy(tc_ugraph *g) {
+    if (!g) return TC_OK;
+    cudaStream_t s = g->ctx ? g->ctx->stream : nullptr;
+    dfree(g->rp, s);
+    dfree(g->col, s);
+    dfree(g->deg, s);
+    dfree(g->rowid, s);
+    delete g;
+    return TC_OK;
+}
+
+int tc_orient(tc_ctx *ctx, const tc_ugraph *ug, int tie, tc_graph **out) {
+    if (!ug || !out || (tie != TC_TIE_REFERENCE && tie != TC_TIE_ID_ASC))
+        return set_error(TC_E_INVALID, "bad orientation arguments");
+    if (!ctx) ctx = ug->ctx;
+    *out = nullptr;
+    cudaStream_t s = ctx->stream;
+    const int64_t V = ug->n_rows, nnz = ug->nnz;
+    DBuf<uint8_t> flags;
+    DBuf<int32_t> pos, orp, ocol;
+    TC_TRY(flags.alloc((size_t)nnz, s));
+    TC_TRY(pos.alloc((size_t)nnz + 1, s));
+    if (nnz) {
+        orient_flags_kernel<<<grid(nnz, ctx), 256, 0, s>>>(ug->rowid, ug->col, ug->deg, nnz, tie, flags.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    TC_TRY(scan_flags_u8(flags.p, pos.p, nnz, s));
+    int32_t m32 = 0;
+    TC_TRY(d2h_scalar(&m32, pos.p + nnz, s));
+    TC_TRY(orp.alloc((size_t)V + 1, s));
+    TC_TRY(ocol.alloc((size_t)std::max<int32_t>(m32, 1), s));
+    if (nnz) {
+        compact_i32_kernel<<<grid(nnz, ctx), 256, 0, s>>>(ug->col, flags.p, pos.p, nnz, ocol.p);
+        TC_CUDA(cudaGetLastError());
+    }
+    gather_rp_kernel<<<grid(V + 1, ctx), 256, 0, s>>>(ug->rp, pos.p, V + 1, orp.p);
+    TC_CUDA(cudaGetLastError());
+    TC_CUDA(cudaStreamSynchronize(s));
+    tc_graph *g = nullptr;
+    TC_TRY(graph_adopt_device(ctx, orp.p, ocol.p, V, m32, V, &g));
+    orp.release();
+    ocol.release();
+    *out = g;
+    return TC_OK;
+}
+
+int tc_graph_from_edges(tc_ctx *ctx, const int64_t *src, const int64_t *dst, int64_t n_edges, int64_t n_nodes, int tie,
+                        tc_graph **out) {
+    tc_ugraph *ug = nullptr;
+    TC_TRY(tc_ugraph_from_edges(ctx, src, dst, n_edges, n_nodes, &ug));
+    const int st = tc_orient(ctx, ug, tie, out);
+    tc_ugraph_destroy(ug);
+    return st;
+}
+
+int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k, int tie, tc_graph **parts_out) {
+    if (!ug || !part || k < 1 || !parts_out || (tie != TC_TIE_REFERENCE && tie != TC_TIE_ID_ASC))
+        return set_error(TC_E_INVALID, "bad halo arguments");
+    if (!ctx) ctx = ug->ctx;
+    for (int p = 0; p < k; ++p) parts_out[p] = nullptr;
+    cudaStream_t s = ctx->stream;
+    const int64_t V = ug->n_rows, nnz = ug->nnz;
+    for (int64_t v = 0; v < V; ++v)
+        if (part[v] < 0 || part[v] >= k) return set_error(TC_E_RANGE, "part[%lld] = %d outside [0, %d)", (long long)v, part[v], k);
+    DBuf<int32_t> dpart, lidP, lidH, lid, cnt, lrp, posP, posH;
+    DBuf<uint8_t> inP, inH, fP, fH;
+    TC_TRY(dpart.alloc((size_t)std::max<int64_t>(V, 1), s));
+    if (V) TC_CUDA(cudaMemcpyAsync(dpart.p, part, sizeof(int32_t) * (size_t)V, cudaMemcpyHostToDevice, s));
+    TC_TRY(inP.alloc((size_t)V, s));
+    TC_TRY(inH.alloc((size_t)V, s));
+    TC_TRY(lidP.alloc((size_t)V + 1, s));
+    TC_TRY(lidH.alloc((size_t)V + 1, s));
+    TC_TRY(lid.alloc((size_t)std::max<int64_t>(V, 1), s));
+    TC_TRY(cnt.alloc((size_t)V + 1, s));
+    TC_TRY(lrp.alloc((size_t)V + 1, s));
+    TC_TRY(fP.alloc((size_t)nnz, s));
+    TC_TRY(fH.alloc((size_t)nnz, s));
+    TC_TRY(posP.alloc((size_t)nnz + 1, s));
+    TC_TRY(posH.alloc((size_t)nnz + 1, s));
+    const int gV = grid(V, ctx), gE = grid(nnz, ctx);
+    int st = TC_OK;
+    for (int p = 0; p < k && st == TC_OK; ++p) {
+        if (V) part_flags_kernel<<<gV, 256, 0, s>>>(dpart.p, V, p, inP.p);
+        TC_CUDA(cudaMemsetAsync(inH.p, 0, (size_t)V, s));
+        if (nnz) halo_flags_kernel<<<gE, 256, 0, s>>>(ug->rowid, ug->col, nnz, dpart.p, p, inH.p);
+        TC_CUDA(cudaGetLastError());
+        TC_TRY(scan_flags_u8(inP.p, lidP.p, V, s));
+        TC_TRY(scan_flags_u8(inH.p, lidH.p, V, s));
+        int32_t t_ver = 0, n_halo = 0;
+        TC_TRY(d2h_scalar(&t_ver, lidP.p + V, s));
+        TC_TRY(d2h_scalar(&n_halo, lidH.p + V, s));
+        const int64_t n_comb = (int64_t)t_ver + n_halo;
+        if (V) local_ids_kernel<<<gV, 256, 0, s>>>(inP.p, inH.p, lidP.p, lidH.p, V, t_ver, lid.p);
+        TC_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * ((size_t)n_comb + 1), s));
+        if (nnz)
+            halo_edge_flags_kernel<<<gE, 256, 0, s>>>(ug->rowid, ug->col, ug->deg, nnz, lid.p, inP.p, tie, fP.p, fH.p,
+                                                      cnt.p);
+        TC_CUDA(cudaGetLastError());
+        TC_TRY(scan_exclusive_i32(cnt.p, lrp.p, n_comb, s));
+        TC_TRY(scan_flags_u8(fP.p, posP.p, nnz, s));
+        TC_TRY(scan_flags_u8(fH.p, posH.p, nnz, s));
+        int32_t lnnz = 0;
+        TC_TRY(d2h_scalar(&lnnz, lrp.p + n_comb, s));
+        DBuf<int32_t> lcol, lrow, indeg, front, next, fn;
+        DBuf<uint8_t> removed;
+        TC_TRY(lcol.alloc((size_t)lnnz, s));
+        TC_TRY(lrow.alloc((size_t)lnnz, s));
+        if (nnz)
+            halo_scatter_kernel<<<gE, 256, 0, s>>>(ug->rowid, ug->col, ug->rp, nnz, lid.p, fP.p, fH.p, posP.p, posH.p,
+                                                   lrp.p, lcol.p, lrow.p);
+        TC_CUDA(cudaGetLastError());
+        // prune: peel halo vertices of zero in-degree until none is left
+        TC_TRY(indeg.alloc((size_t)std::max<int64_t>(n_comb, 1), s));
+        TC_TRY(removed.alloc((size_t)std::max<int64_t>(n_comb, 1), s));
+        TC_TRY(front.alloc((size_t)std::max<int32_t>(n_halo, 1), s));
+        TC_TRY(next.alloc((size_t)std::max<int32_t>(n_halo, 1), s));
+        TC_TRY(fn.alloc(2, s));
+        TC_CUDA(cudaMemsetAsync(indeg.p, 0, sizeof(int32_t) * (size_t)std::max<int64_t>(n_comb, 1), s));
+        TC_CUDA(cudaMemsetAsync(removed.p, 0, (size_t)std::max<int64_t>(n_comb, 1), s));
+        TC_CUDA(cudaMemsetAsync(fn.p, 0, 2 * sizeof(int32_t), s));
+        if (lnnz) indeg_kernel<<<grid(lnnz, ctx), 256, 0, s>>>(lcol.p, lnnz, indeg.p);
+        if (n_comb) frontier_init_kernel<<<grid(n_comb, ctx), 256, 0, s>>>(indeg.p, n_comb, t_ver, removed.p, front.p, fn.p);
+        TC_CUDA(cudaGetLastError());
+        int32_t n_front = 0, n_removed = 0;
+        TC_TRY(d2h_scalar(&n_front, fn.p, s));
+        // each round removes at least one halo vertex, so at most n_halo rounds
+        for (int round = 0; n_front > 0 && round <= n_halo; ++round) {
+            n_removed += n_front;
+            TC_CUDA(cudaMemsetAsync(fn.p + 1, 0, sizeof(int32_t), s));
+            peel_kernel<<<grid((int64_t)n_front * 32, ctx), 256, 0, s>>>(front.p, n_front, lrp.p, lcol.p, t_ver, indeg.p,
+                                                                         removed.p, next.p, fn.p + 1);
+            TC_CUDA(cudaGetLastError());
+            TC_TRY(d2h_scalar(&n_front, fn.p + 1, s));
+            std::swap(front.p, next.p);
+        }
+        int32_t *out_rp = nullptr, *out_col = nullptr;
+        int64_t n_local = n_comb, out_nnz = lnnz;
+        if (n_removed == 0) {
+            DBuf<int32_t> rp_copy;
+            TC_TRY(rp_copy.alloc((size_t)n_comb + 1, s));
+            TC_CUDA(cudaMemcpyAsync(rp_copy.p, lrp.p, sizeof(int32_t) * ((size_t)n_comb + 1), cudaMemcpyDeviceToDevice, s));
+            out_rp = rp_copy.release();
+            out_col = lcol.release();
+        } else {
+            DBuf<uint8_t> alive;
+            DBuf<int32_t> len, nid, newpos, rp2, col2;
+            TC_TRY(alive.alloc((size_t)n_comb, s));
+            TC_TRY(len.alloc((size_t)n_comb, s));
+            TC_TRY(nid.alloc((size_t)n_comb + 1, s));
+            TC_TRY(newpos.alloc((size_t)n_comb + 1, s));
+            alive_kernel<<<grid(n_comb, ctx), 256, 0, s>>>(removed.p, lrp.p, n_comb, alive.p, len.p);
+            TC_CUDA(cudaGetLastError());
+            TC_TRY(scan_flags_u8(alive.p, nid.p, n_comb, s));
+            TC_TRY(scan_exclusive_i32(len.p, newpos.p, n_comb, s));
+            int32_t nl = 0, nn = 0;
+            TC_TRY(d2h_scalar(&nl, nid.p + n_comb, s));
+            TC_TRY(d2h_scalar(&nn, newpos.p + n_comb, s));
+            n_local = nl;
+            out_nnz = nn;
+            TC_TRY(rp2.alloc((size_t)nl + 1, s));
+            TC_TRY(col2.alloc((size_t)std::max(nn, 1), s));
+            prune_rows_kernel<<<grid(n_comb, ctx), 256, 0, s>>>(alive.p, nid.p, newpos.p, n_comb, rp2.p);
+            TC_CUDA(cudaMemcpyAsync(rp2.p + nl, &nn, sizeof(int32_t), cudaMemcpyHostToDevice, s));
+            if (lnnz)
+                prune_cols_kernel<<<grid(lnnz, ctx), 256, 0, s>>>(lrow.p, lcol.p, lrp.p, lnnz, alive.p, nid.p, newpos.p,
+                                                                  col2.p);
+            TC_CUDA(cudaGetLastError());
+            TC_CUDA(cudaStreamSynchronize(s));
+            out_rp = rp2.release();
+            out_col = col2.release();
+        }
+        TC_CUDA(cudaStreamSynchronize(s));
+        st = graph_adopt_device(ctx, out_rp, out_col, n_local, out_nnz, t_ver, &parts_out[p]);
+        if (st != TC_OK) {
+            dfree(out_rp, s);
+            dfree(out_col, s);
+        }
+    }
+    if (st != TC_OK)
+        for (int p = 0; p < k; ++p) {
+            tc_graph_destroy(parts_out[p]);
+            parts_out[p] = nullptr;
+        }
+    return st;
+}
+
+}  // extern "C"
