@@ -1,0 +1,367 @@
+"""Benchmark: exact triangle counting throughput (oriented edges/s) on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload rmat21|road|rmat16|rmat23]
+
+One step = one exact count of the workload graph (classify + persistent count
+kernel, result in device memory).  Default workload: R-MAT scale 21, edge
+factor 16, (a, b, c) = (0.57, 0.19, 0.19), seeded and vertex-permuted,
+cleaned and degree-oriented on the device (the plain TC_128 path on the
+"two shapes on one GB300" configuration, shape a).
+
+Printed on rank 0 as ONE JSON line:
+  value      whole-job oriented edges/s with the graph resident in HBM, L2
+             flushed (512 MiB memset) before every timed step, CUDA events on
+             the launching stream, max over ranks
+  e2e        the same metric through the C ABI (tc_count_csr_i32) from pinned
+             host buffers: upload + validation + count + result read-back
+  roofline   algorithmic bytes of the count per launch
+             B = 4(V+1) + 12|E+| + 4 W+ + 8 (W+ = sum over oriented edges of
+             d+(v)) / kernel time, against the measured HBM copy peak
+  cpu_baseline  the OpenMP merge-intersection oracle on the machine's host cores
+  reference_gpu_kernel  the reference's own TC_128 kernel (built from its
+             sources for sm_103a) on the same graph and GPU, when available
+
+--impl reference times the reference's CPU path on the host cores: the
+OpenMP oracle restatement (the reference's counting code is CUDA only; its
+CPU orientation tool has no counter), one bounded sample of roots per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "oriented edges/s"
+UNIT = "edges/s"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["rmat21", "road", "rmat16", "rmat18", "rmat23"], default="rmat21")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--no-ref-kernel", action="store_true")
+    return ap.parse_args()
+
+
+def workload_edges(name: str):
+    from trianglecount_gb300 import generators as gen
+    if name.startswith("rmat"):
+        scale = int(name[4:])
+        src, dst = gen.rmat(scale, 16)
+        return src, dst, {"workload": f"rmat{scale}_ef16_plain", "generator": "R-MAT", "scale": scale,
+                          "edge_factor": 16, "abc": [gen.RMAT_A, gen.RMAT_B, gen.RMAT_C],
+                          "seed": gen.SEED.get(f"rmat{scale}", 0), "vertex_permutation": True}
+    src, dst = gen.road()
+    return src, dst, {"workload": "road_1448x1448_plain", "generator": "jittered grid",
+                      "side": gen.ROAD_SIDE, "p_delete": gen.ROAD_P_DELETE, "diag_rate": gen.ROAD_DIAG_RATE,
+                      "seed": gen.SEED["road"]}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def max_over_ranks(x: float, pg, device) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def run_reference(args, world, rank):
+    """CPU path of the reference (OpenMP oracle restatement), rank 0 only."""
+    if rank != 0:
+        return
+    import oracle
+    src, dst, cfg = workload_edges(args.workload)
+    orp, ocl, _ = oracle.pipeline(src, dst)
+    V = len(orp) - 1
+    n_samples = 8
+    bounds = [V * i // n_samples for i in range(n_samples + 1)]
+    times, edges = [], []
+    for step in range(args.warmup + args.steps):
+        i = step % n_samples
+        r0, r1 = bounds[i], bounds[i + 1]
+        t0 = time.perf_counter()
+        oracle.count_range_i32(orp, ocl, r0, r1)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+            edges.append(int(orp[r1] - orp[r0]))
+    value = sum(edges) / sum(times)
+    cores = oracle.num_threads()
+    cfg.update({"V": V, "oriented_edges": int(len(ocl))})
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic", "config": cfg,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"one 1/{n_samples} slice of the roots per step (permuted ids), "
+                                   "OpenMP merge intersection, schedule(dynamic,64)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def load_traffic(workload: str):
+    p = os.path.join(ROOT, "profiles", f"count_kernel_{workload}.traffic.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except ValueError:
+            return None
+    return None
+
+
+def run_ours(args, world, rank, local, pg):
+    import torch
+
+    import trianglecount_gb300 as tc
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    ctx = tc.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+
+    src, dst, cfg = workload_edges(args.workload)
+    t0 = time.perf_counter()
+    g = ctx.graph_from_edges(src, dst)
+    prep_s = time.perf_counter() - t0
+    rp, col = g.download()
+    V, E = len(rp) - 1, len(col)
+    dplus = np.diff(rp).astype(np.int64)
+    W = int(dplus[col].sum())
+    B_alg = 4 * (V + 1) + 12 * E + 4 * W + 8
+
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    d_out = torch.zeros(1, dtype=torch.int64, device=dev)
+    lib = tc.lib()
+
+    def one_step(e0, e1):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0.record(stream)
+            st = lib.tc_count_async(ctx.handle, g.handle, d_out.data_ptr())
+            e1.record(stream)
+        if st != 0:
+            raise tc.TCError(st, "tc_count_async", lib.tc_last_error().decode())
+
+    for _ in range(args.warmup):
+        one_step(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+    torch.cuda.synchronize()
+    count = int(d_out.item())
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(pg)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for e0, e1 in evs:
+        one_step(e0, e1)
+    torch.cuda.synchronize()
+    barrier(pg)
+    clk = clocks.stop()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    ms = max_over_ranks(sum(step_ms) / len(step_ms), pg, dev)
+    value = world * E / (ms / 1000.0)
+    assert int(d_out.item()) == count
+
+    # ---- end to end through the C ABI from pinned host memory ----
+    rp_h = torch.from_numpy(rp).pin_memory()
+    col_h = torch.from_numpy(col).pin_memory()
+    out = np.zeros(1, np.uint64)
+    import ctypes as C
+    e2e_ms = []
+    for step in range(args.warmup + args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0.record(stream)
+        st = lib.tc_count_csr_i32(ctx.handle, C.c_void_p(rp_h.data_ptr()), C.c_void_p(col_h.data_ptr()), V, E,
+                                  out.ctypes.data_as(C.POINTER(C.c_uint64)))
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        if st != 0:
+            raise tc.TCError(st, "tc_count_csr_i32", lib.tc_last_error().decode())
+        e1.synchronize()
+        if step >= args.warmup:
+            e2e_ms.append(e0.elapsed_time(e1))
+        assert int(out[0]) == count
+    e2e = max_over_ranks(sum(e2e_ms) / len(e2e_ms), pg, dev)
+
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak = float(json.load(open(peaks_path))["hbm_gbs"])
+        peak_src = "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = B_alg / (ms / 1000.0) / 1e9
+    tr = load_traffic(cfg["workload"])
+
+    res = None
+    if rank == 0:
+        cfg.update({"V": V, "oriented_edges": E, "undirected_edges": E, "W_plus": W, "triangles": count,
+                    "tie_break": "reference (deg u < deg w, or equal and w < u)", "index_type": "int32",
+                    "l2": "flushed before every timed step (512 MiB memset on the launching stream)",
+                    "device_preprocess_s": round(prep_s, 3), "parallelism": f"replicas x{world}"})
+        res = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded R-MAT / grid generators)",
+            "config": cfg,
+            "gpu_launches": 2 * args.steps,
+            "e2e": {"value": world * E / (e2e / 1000.0), "unit": UNIT, "ms_per_step": e2e,
+                    "h2d_bytes_per_step": 4 * (V + 1) + 4 * E, "d2h_bytes_per_step": 8 + 8 + 24,
+                    "path": "tc_count_csr_i32 (upload + validate + count + read-back)",
+                    "gpu_launches": 4 * args.steps},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": f"{peak_src} hbm_gbs (copy, burst)",
+                         "algorithmic_bytes_per_launch": B_alg,
+                         "traffic": (tr or {}).get("traffic_bytes_per_launch"),
+                         "traffic_source": (tr or {}).get("source")},
+            "clocks": clk,
+        }
+        if not args.no_ref_kernel:
+            try:
+                import oracle
+                if oracle.ref_kernel_available():
+                    pr, _ = oracle.ref_tc128(rp, col, runs=1)
+                    ref_ms = []
+                    for _ in range(3):
+                        flush.zero_()
+                        torch.cuda.synchronize()
+                        pr, t_ms = oracle.ref_tc128(rp, col, runs=1)
+                        ref_ms.append(t_ms)
+                    ok = int(pr.sum()) == count
+                    rms = statistics.median(ref_ms)
+                    res["reference_gpu_kernel"] = {
+                        "value": E / (rms / 1000.0), "unit": UNIT, "ms": rms, "count_matches": ok,
+                        "source": "TC_128 Find_Triangle (ShareKernelTCV62_update_v1.cu) built from the reference "
+                                  "sources for sm_103a, one 128-thread block per vertex, median of 3, L2 flushed",
+                        "speedup_of_ours": rms / ms}
+            except Exception as ex:  # reported, never fatal
+                res["reference_gpu_kernel"] = {"unavailable": str(ex)[:200]}
+        if not args.no_cpu:
+            import oracle
+            t0 = time.perf_counter()
+            ccount = oracle.count(rp, col)
+            cdt = time.perf_counter() - t0
+            res["cpu_baseline"] = {"value": E / cdt, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+                                   "sample": "the whole graph, one full count (OpenMP merge intersection, "
+                                             "schedule(dynamic,64), u64 reduction)",
+                                   "seconds": cdt, "count_matches": ccount == count}
+    barrier(pg)
+    ctx.close()
+    return res
+
+
+def main():
+    args = parse()
+    world, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        res = run_ours(args, world, rank, local, pg)
+        if rank == 0:
+            print(json.dumps(res), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

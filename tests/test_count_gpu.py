@@ -125,3 +125,18 @@ def test_end_to_end_host_csr_and_repeatability(ctx):
     assert ctx.count_csr(orp, ocl) == want
     g = ctx.upload(orp, ocl)
     assert {ctx.count(g) for _ in range(5)} == {want}
+
+
+def test_context_outlives_its_graphs():
+    """Closing a context while graphs / batches are alive defers its release
+    until the last of them is freed (reference counting in the C ABI)."""
+    src, dst = gen.rmat(10)
+    orp, ocl, want = oracle.pipeline(src, dst)
+    c = tc.Context(0)
+    g = c.upload(orp, ocl)
+    b = c.batch([g])
+    c.close()
+    assert list(b.run()) == [want]
+    assert g.count() == want
+    b.free()
+    g.free()

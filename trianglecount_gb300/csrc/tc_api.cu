@@ -126,7 +126,11 @@ int enqueue_graph_count(tc_graph *g, unsigned long long *per_root, unsigned long
     d.n_roots = g->n_roots;
     d.chunk_base = 0;
     d.per_root = per_root;
-    TC_CUDA(cudaMemcpyAsync(g->d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, ctx->stream));
+    if (!g->desc_valid || memcmp(&d, &g->desc_on_device, sizeof(d)) != 0) {
+        TC_CUDA(cudaMemcpyAsync(g->d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, ctx->stream));
+        g->desc_on_device = d;
+        g->desc_valid = true;
+    }
     const int64_t chunks = (g->n_roots + 31) / 32;
     return launch_count(g->d_desc, 1, chunks, g->d_heavy, g->heavy_cap, g->d_work, results ? results : g->d_result,
                         ctx->tuned, ctx->stream, launches);
@@ -142,6 +146,7 @@ int new_graph(tc_ctx *ctx, int64_t n_rows, int64_t nnz, int64_t n_roots, tc_grap
                          (long long)nnz);
     tc_graph *g = new tc_graph();
     g->ctx = ctx;
+    ctx_retain(ctx);
     g->n_rows = n_rows;
     g->nnz = nnz;
     g->n_roots = n_roots;
@@ -183,6 +188,21 @@ int dalloc(void **p, size_t bytes, cudaStream_t s) {
 
 void dfree(void *p, cudaStream_t s) {
     if (p) cudaFreeAsync(p, s);
+}
+
+void ctx_retain(tc_ctx *c) {
+    if (c) c->refs.fetch_add(1);
+}
+
+void ctx_release(tc_ctx *c) {
+    if (!c || c->refs.fetch_sub(1) != 1) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
 }
 
 int device_sm_count(int device) {
@@ -278,14 +298,7 @@ int tc_ctx_create(int device, tc_ctx **out) {
 }
 
 int tc_ctx_destroy(tc_ctx *c) {
-    if (!c) return TC_OK;
-    cudaSetDevice(c->device);
-    if (c->stream) cudaStreamSynchronize(c->stream);
-    for (auto &e : c->ev)
-        if (e) cudaEventDestroy(e);
-    if (c->h_pinned) cudaFreeHost(c->h_pinned);
-    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
-    delete c;
+    ctx_release(c);  // freed now, or when its last graph / batch is destroyed
     return TC_OK;
 }
 
@@ -446,7 +459,9 @@ int tc_graph_destroy(tc_graph *g) {
     dfree(g->d_desc, s);
     dfree(g->d_work, s);
     dfree(g->d_heavy, s);
+    tc_ctx *ctx = g->ctx;
     delete g;
+    ctx_release(ctx);
     return TC_OK;
 }
 
@@ -550,7 +565,9 @@ int tc_batch_destroy(tc_batch *b) {
     dfree(b->d_heavy, s);
     dfree(b->d_work, s);
     if (b->h_out) cudaFreeHost(b->h_out);
+    tc_ctx *ctx = b->ctx;
     delete b;
+    ctx_release(ctx);
     return TC_OK;
 }
 
@@ -559,6 +576,7 @@ int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out)
     *out = nullptr;
     tc_batch *b = new tc_batch();
     b->ctx = ctx;
+    ctx_retain(ctx);
     b->n = n;
     cudaStream_t s = ctx->stream;
     std::vector<GraphDesc> desc((size_t)n);

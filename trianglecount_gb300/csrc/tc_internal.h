@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 
 #include "tc.h"
@@ -115,6 +116,12 @@ int radix_sort_u64(uint64_t **keys, uint64_t **tmp, int64_t n, int bits, cudaStr
 
 int device_sm_count(int device);
 
+// Context lifetime: every graph, ugraph and batch holds a reference to its
+// context, so tc_ctx_destroy only drops the caller's reference and the
+// context is freed when its last object is destroyed.
+void ctx_retain(tc_ctx *c);
+void ctx_release(tc_ctx *c);
+
 }  // namespace tc
 
 // ---- library object layouts ----------------------------------------------------------
@@ -127,6 +134,7 @@ struct tc_ctx {
     tc::Tuned tuned{};
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     unsigned long long *h_pinned = nullptr;  // small pinned read-back area
+    std::atomic<int> refs{1};                // the handle + one per live object
 };
 
 struct tc_graph {
@@ -141,6 +149,8 @@ struct tc_graph {
     unsigned long long *d_result = nullptr;
     tc::HeavyEntry *d_heavy = nullptr;
     int64_t heavy_cap = 0;
+    tc::GraphDesc desc_on_device{};  // what d_desc holds (skip re-uploads)
+    bool desc_valid = false;
 };
 
 struct tc_ugraph {

@@ -288,6 +288,7 @@ int finish_ugraph(tc_ctx *ctx, int32_t *rp, int32_t *col, int32_t *deg, int32_t 
                   tc_ugraph **out) {
     tc_ugraph *g = new tc_ugraph();
     g->ctx = ctx;
+    ctx_retain(ctx);
     g->rp = rp;
     g->col = col;
     g->deg = deg;
@@ -485,7 +486,9 @@ int tc_ugraph_destroy(tc_ugraph *g) {
     dfree(g->col, s);
     dfree(g->deg, s);
     dfree(g->rowid, s);
+    tc_ctx *ctx = g->ctx;
     delete g;
+    ctx_release(ctx);
     return TC_OK;
 }
 
