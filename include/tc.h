@@ -82,16 +82,20 @@ TC_API int tc_ctx_synchronize(tc_ctx *ctx);
 TC_API int tc_ctx_device_info(tc_ctx *ctx, int *sm_count, size_t *free_bytes, size_t *total_bytes);
 
 /* Strategy thresholds of the counting kernel (picked by the autotuner).
- * Roots u with 2 <= d+(u) <= warp_max_deg are counted by one warp with a
- * shared-memory hash of N+(u); larger roots are split into block units of
- * block_slice out-neighbours, each probing a shared hash of one tile of N+(u).
- * Roots with d+(u) <= tiny_max_deg use a register-broadcast compare instead of
- * the hash.  In tc_ctx_set_tuning, warp_max_deg / block_slice <= 0 and
- * tiny_max_deg / blocks_per_sm < 0 keep the current value. */
+ * The classifier computes, per root u, d+(u) and its work
+ * w(u) = sum_{v in N+(u)} d+(v) (one probe per oriented wedge).  Light roots
+ * (d+(u) <= warp_max_deg and w(u) <= light_max_work) are counted by one warp
+ * with a per-warp shared-memory hash of N+(u); heavy roots are split into
+ * block units of about unit_work probes, each probing a shared hash of one
+ * tile of N+(u).  Per out-neighbour v, lists with d+(v) >= long_list are
+ * streamed by the whole warp; shorter lists are flattened across the lanes.
+ * In tc_ctx_set_tuning, fields <= 0 (long_list, blocks_per_sm: < 0) keep
+ * the current value. */
 typedef struct tc_tuning {
-    int32_t warp_max_deg;   /* 32..1024, power of two */
-    int32_t block_slice;    /* out-neighbours per block unit, multiple of 32 */
-    int32_t tiny_max_deg;   /* 0..32 */
+    int32_t warp_max_deg;   /* 32..512, power of two */
+    int32_t light_max_work; /* wedge probes a light root may have */
+    int32_t unit_work;      /* target wedge probes per heavy block unit */
+    int32_t long_list;      /* 0..4096 */
     int32_t blocks_per_sm;  /* persistent grid = SMs * this (0: occupancy) */
 } tc_tuning;
 TC_API int tc_ctx_get_tuning(tc_ctx *ctx, tc_tuning *out);

@@ -14,9 +14,9 @@ pytestmark = pytest.mark.gpu
 
 TUNINGS = [
     {},  # defaults
-    {"warp_max_deg": 32, "block_slice": 32, "tiny_max_deg": 0},   # heavy path everywhere, tiny slices
-    {"warp_max_deg": 1024, "block_slice": 2048, "tiny_max_deg": 32},
-    {"warp_max_deg": 64, "block_slice": 96, "tiny_max_deg": 4, "blocks_per_sm": 1},
+    {"warp_max_deg": 32, "light_max_work": 1, "unit_work": 1, "long_list": 0},  # heavy path everywhere, 32-v slices
+    {"warp_max_deg": 512, "light_max_work": 1 << 30, "unit_work": 1 << 30, "long_list": 4096},  # warps only, flattened
+    {"warp_max_deg": 64, "light_max_work": 500, "unit_work": 3000, "long_list": 5, "blocks_per_sm": 1},
 ]
 
 
@@ -24,7 +24,7 @@ TUNINGS = [
 def tuned(ctx):
     old = ctx.get_tuning()
     yield ctx
-    ctx.set_tuning(old["warp_max_deg"], old["block_slice"], old["tiny_max_deg"], 0)
+    ctx.set_tuning(old["warp_max_deg"], old["light_max_work"], old["unit_work"], old["long_list"], 0)
 
 
 @pytest.mark.parametrize("tuning", TUNINGS)

@@ -206,9 +206,9 @@ class Context:
         N.call("tc_ctx_get_tuning", self._h, C.byref(t))
         return {k: getattr(t, k) for k, _ in N.Tuning._fields_}
 
-    def set_tuning(self, warp_max_deg: int = 0, block_slice: int = 0, tiny_max_deg: int = -1,
+    def set_tuning(self, warp_max_deg: int = 0, light_max_work: int = 0, unit_work: int = 0, long_list: int = -1,
                    blocks_per_sm: int = -1) -> None:
-        t = N.Tuning(warp_max_deg, block_slice, tiny_max_deg, blocks_per_sm)
+        t = N.Tuning(warp_max_deg, light_max_work, unit_work, long_list, blocks_per_sm)
         N.call("tc_ctx_set_tuning", self._h, C.byref(t))
 
     # ---- graphs ----

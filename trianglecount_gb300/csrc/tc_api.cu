@@ -100,13 +100,15 @@ int check_graph(const tc_graph *g) {
 // Count scratch of a graph: descriptor, work words + result, heavy list.
 int ensure_count_scratch(tc_graph *g) {
     tc_ctx *ctx = g->ctx;
-    const int64_t cap = g->nnz / (ctx->tuned.warp_max + 1) + 1;
+    // one entry per heavy root at most; heavy roots have d+(u) >= 2
+    const int64_t cap = std::min(g->n_roots, g->nnz / 2) + 1;
     if (!g->d_work) {
         void *p = nullptr;
         TC_TRY(dalloc(&p, sizeof(CountWork) + sizeof(unsigned long long), ctx->stream));
         g->d_work = (CountWork *)p;
         g->d_result = (unsigned long long *)(g->d_work + 1);
         TC_TRY(dalloc((void **)&g->d_desc, sizeof(GraphDesc), ctx->stream));
+        TC_TRY(dalloc((void **)&g->d_mask, sizeof(uint32_t) * (size_t)((g->n_roots + 31) / 32 + 1), ctx->stream));
     }
     if (g->heavy_cap < cap) {
         if (g->d_heavy) dfree(g->d_heavy, ctx->stream);
@@ -132,8 +134,8 @@ int enqueue_graph_count(tc_graph *g, unsigned long long *per_root, unsigned long
         g->desc_valid = true;
     }
     const int64_t chunks = (g->n_roots + 31) / 32;
-    return launch_count(g->d_desc, 1, chunks, g->d_heavy, g->heavy_cap, g->d_work, results ? results : g->d_result,
-                        ctx->tuned, ctx->stream, launches);
+    return launch_count(g->d_desc, 1, chunks, g->d_heavy, g->heavy_cap, g->d_mask, g->d_work,
+                        results ? results : g->d_result, ctx->tuned, ctx->stream, launches);
 }
 
 int new_graph(tc_ctx *ctx, int64_t n_rows, int64_t nnz, int64_t n_roots, tc_graph **out) {
@@ -278,8 +280,9 @@ int tc_ctx_create(int device, tc_ctx **out) {
     c->device = device;
     c->sm_count = device_sm_count(device);
     c->tuning.warp_max_deg = 128;
-    c->tuning.block_slice = 512;
-    c->tuning.tiny_max_deg = 8;
+    c->tuning.light_max_work = 32768;
+    c->tuning.unit_work = 65536;
+    c->tuning.long_list = 16;
     c->tuning.blocks_per_sm = 0;
     int st = TC_OK;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) st = TC_E_CUDA;
@@ -341,8 +344,9 @@ int tc_ctx_set_tuning(tc_ctx *c, const tc_tuning *in) {
     if (!c || !in) return set_error(TC_E_INVALID, "null argument");
     tc_tuning t = c->tuning;
     if (in->warp_max_deg > 0) t.warp_max_deg = in->warp_max_deg;
-    if (in->block_slice > 0) t.block_slice = in->block_slice;
-    if (in->tiny_max_deg >= 0) t.tiny_max_deg = in->tiny_max_deg;
+    if (in->light_max_work > 0) t.light_max_work = in->light_max_work;
+    if (in->unit_work > 0) t.unit_work = in->unit_work;
+    if (in->long_list >= 0) t.long_list = in->long_list;
     if (in->blocks_per_sm >= 0) t.blocks_per_sm = in->blocks_per_sm;
     Tuned r;
     TC_TRY(resolve_tuning(t, c->sm_count, &r));
@@ -459,6 +463,7 @@ int tc_graph_destroy(tc_graph *g) {
     dfree(g->d_desc, s);
     dfree(g->d_work, s);
     dfree(g->d_heavy, s);
+    dfree(g->d_mask, s);
     tc_ctx *ctx = g->ctx;
     delete g;
     ctx_release(ctx);
@@ -546,6 +551,7 @@ struct tc_batch {
     GraphDesc *d_desc = nullptr;
     HeavyEntry *d_heavy = nullptr;
     int64_t heavy_cap = 0;
+    uint32_t *d_mask = nullptr;
     CountWork *d_work = nullptr;  // followed by n results
     unsigned long long *h_out = nullptr;  // pinned: CountWork + n results
     int64_t total_chunks = 0;
@@ -563,6 +569,7 @@ int tc_batch_destroy(tc_batch *b) {
     if (b->graph) cudaGraphDestroy(b->graph);
     dfree(b->d_desc, s);
     dfree(b->d_heavy, s);
+    dfree(b->d_mask, s);
     dfree(b->d_work, s);
     if (b->h_out) cudaFreeHost(b->h_out);
     tc_ctx *ctx = b->ctx;
@@ -594,12 +601,13 @@ int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out)
         desc[i].chunk_base = chunks;
         desc[i].per_root = nullptr;
         chunks += (g->n_roots + 31) / 32;
-        cap += g->nnz / (ctx->tuned.warp_max + 1) + 1;
+        cap += std::min(g->n_roots, g->nnz / 2) + 1;
     }
     b->total_chunks = chunks;
     b->heavy_cap = cap;
     int st = dalloc((void **)&b->d_desc, sizeof(GraphDesc) * (size_t)n, s);
     if (st == TC_OK) st = dalloc((void **)&b->d_heavy, sizeof(HeavyEntry) * (size_t)cap, s);
+    if (st == TC_OK) st = dalloc((void **)&b->d_mask, sizeof(uint32_t) * (size_t)(chunks + 1), s);
     if (st == TC_OK) st = dalloc((void **)&b->d_work, sizeof(CountWork) + sizeof(unsigned long long) * (size_t)n, s);
     if (st == TC_OK && cudaMallocHost(&b->h_out, sizeof(CountWork) + sizeof(unsigned long long) * (size_t)n) != cudaSuccess)
         st = set_error(TC_E_NOMEM, "pinned result buffer");
@@ -611,7 +619,7 @@ int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out)
     if (st == TC_OK && cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         st = set_error(TC_E_CUDA, "stream capture could not start");
     if (st == TC_OK) {
-        int ls = launch_count(b->d_desc, n, chunks, b->d_heavy, cap, b->d_work,
+        int ls = launch_count(b->d_desc, n, chunks, b->d_heavy, cap, b->d_mask, b->d_work,
                               (unsigned long long *)(b->d_work + 1), ctx->tuned, s, nullptr);
         cudaError_t e = cudaStreamEndCapture(s, &b->graph);
         if (ls != TC_OK) st = ls;

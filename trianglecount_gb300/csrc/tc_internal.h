@@ -73,7 +73,7 @@ struct GraphDesc {
 };
 
 struct HeavyEntry {
-    int32_t g, u, unit_base, n_units;
+    int32_t g, u, unit_base, n_slices;  // units = ceil(d+(u) / tile) * n_slices
 };
 
 // Per-launch device words, zeroed by one memset before each count.
@@ -86,23 +86,26 @@ struct CountWork {
 };
 
 struct Tuned {  // resolved tc_tuning with derived table geometry
-    int warp_max;      // power of two
+    int warp_max;        // power of two
     int log_warp_slots;
-    int slice;
-    int tile;          // block table entries per tile
+    int light_max_work;
+    int unit_work;
+    int long_list;
+    int tile;            // block table entries per tile (a quarter of its slots)
     int log_block_slots;
-    int tiny_max;
-    int threads;       // per block
-    int blocks;        // persistent grid
-    size_t smem;       // dynamic shared memory bytes
+    int threads;         // per block
+    int blocks;          // persistent grid
+    size_t smem;         // dynamic shared memory bytes
 };
 
 int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out);
 
 // Enqueues classify + persistent count for n_graphs descriptors on stream s.
 // results[n_graphs] receives the per-graph totals (zeroed here).
+// light_mask holds one word per 32-root chunk (total_chunks words).
 int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, HeavyEntry *heavy, int64_t heavy_cap,
-                 CountWork *work, unsigned long long *results, const Tuned &tn, cudaStream_t s, int *launches);
+                 uint32_t *light_mask, CountWork *work, unsigned long long *results, const Tuned &tn, cudaStream_t s,
+                 int *launches);
 
 // ---- scans and sort (tc_scan.cu, tc_sort.cu) ----------------------------------------
 // Exclusive scan of n values into out[0..n] (out[n] = total).  out may alias in.
@@ -149,6 +152,7 @@ struct tc_graph {
     unsigned long long *d_result = nullptr;
     tc::HeavyEntry *d_heavy = nullptr;
     int64_t heavy_cap = 0;
+    uint32_t *d_mask = nullptr;          // light-root mask, one word per 32 roots
     tc::GraphDesc desc_on_device{};  // what d_desc holds (skip re-uploads)
     bool desc_valid = false;
 };
