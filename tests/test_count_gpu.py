@@ -67,7 +67,7 @@ def test_graph_families_match_oracle(ctx, maker, tie):
     g = ctx.upload(orp, ocl)
     got, st = ctx.count(g, stats=True)
     assert got == want
-    assert st["launches"] == 2 and st["count_ms"] > 0
+    assert st["launches"] >= 4 and st["count_ms"] > 0
 
 
 def test_rmat_golden_counts_on_device(ctx, golden_dir):

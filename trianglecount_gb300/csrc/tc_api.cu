@@ -97,24 +97,17 @@ int check_graph(const tc_graph *g) {
     return TC_OK;
 }
 
-// Count scratch of a graph: descriptor, work words + result, heavy list.
+// Count scratch of a graph: descriptor, work words + result, CountScratch.
 int ensure_count_scratch(tc_graph *g) {
     tc_ctx *ctx = g->ctx;
-    // one entry per heavy root at most; heavy roots have d+(u) >= 2
-    const int64_t cap = std::min(g->n_roots, g->nnz / 2) + 1;
     if (!g->d_work) {
         void *p = nullptr;
         TC_TRY(dalloc(&p, sizeof(CountWork) + sizeof(unsigned long long), ctx->stream));
         g->d_work = (CountWork *)p;
         g->d_result = (unsigned long long *)(g->d_work + 1);
         TC_TRY(dalloc((void **)&g->d_desc, sizeof(GraphDesc), ctx->stream));
-        TC_TRY(dalloc((void **)&g->d_mask, sizeof(uint32_t) * (size_t)((g->n_roots + 31) / 32 + 1), ctx->stream));
-    }
-    if (g->heavy_cap < cap) {
-        if (g->d_heavy) dfree(g->d_heavy, ctx->stream);
-        g->d_heavy = nullptr;
-        TC_TRY(dalloc((void **)&g->d_heavy, sizeof(HeavyEntry) * (size_t)cap, ctx->stream));
-        g->heavy_cap = cap;
+        TC_TRY(scratch_alloc(&g->sc, g->n_rows + 1, (g->n_rows + 31) / 32, g->nnz,
+                             std::min(g->n_rows, g->nnz) + 1, ctx->stream));
     }
     return TC_OK;
 }
@@ -123,19 +116,22 @@ int enqueue_graph_count(tc_graph *g, unsigned long long *per_root, unsigned long
     tc_ctx *ctx = g->ctx;
     TC_TRY(ensure_count_scratch(g));
     GraphDesc d;
+    memset(&d, 0, sizeof d);
     d.rp = g->rp;
     d.col = g->col;
+    d.n_rows = g->n_rows;
     d.n_roots = g->n_roots;
     d.chunk_base = 0;
+    d.vbase = 0;
     d.per_root = per_root;
     if (!g->desc_valid || memcmp(&d, &g->desc_on_device, sizeof(d)) != 0) {
         TC_CUDA(cudaMemcpyAsync(g->d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, ctx->stream));
         g->desc_on_device = d;
         g->desc_valid = true;
     }
-    const int64_t chunks = (g->n_roots + 31) / 32;
-    return launch_count(g->d_desc, 1, chunks, g->d_heavy, g->heavy_cap, g->d_mask, g->d_work,
-                        results ? results : g->d_result, ctx->tuned, ctx->stream, launches);
+    const int64_t chunks = (g->n_rows + 31) / 32;
+    return launch_count(g->d_desc, 1, chunks, g->n_rows + 1, g->sc, g->d_work, results ? results : g->d_result,
+                        per_root != nullptr, ctx->tuned, ctx->stream, launches);
 }
 
 int new_graph(tc_ctx *ctx, int64_t n_rows, int64_t nnz, int64_t n_roots, tc_graph **out) {
@@ -205,6 +201,29 @@ void ctx_release(tc_ctx *c) {
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
+}
+
+int scratch_alloc(CountScratch *sc, int64_t V, int64_t C, int64_t E, int64_t heavy_cap, cudaStream_t s) {
+    sc->heavy_cap = heavy_cap;
+    TC_TRY(dalloc((void **)&sc->heavy, sizeof(HeavyEntry) * (size_t)std::max<int64_t>(heavy_cap, 1), s));
+    TC_TRY(dalloc((void **)&sc->light_mask, sizeof(uint32_t) * (size_t)std::max<int64_t>(C, 1), s));
+    TC_TRY(dalloc((void **)&sc->in_cnt, sizeof(int32_t) * (size_t)std::max<int64_t>(V, 1), s));
+    TC_TRY(dalloc((void **)&sc->in_off, sizeof(int32_t) * (size_t)(V + 1), s));
+    TC_TRY(dalloc((void **)&sc->in_work, sizeof(unsigned long long) * (size_t)std::max<int64_t>(V, 1), s));
+    TC_TRY(dalloc((void **)&sc->out_work, sizeof(unsigned long long) * (size_t)std::max<int64_t>(V, 1), s));
+    TC_TRY(dalloc((void **)&sc->in_list, sizeof(int32_t) * (size_t)std::max<int64_t>(E, 1), s));
+    return TC_OK;
+}
+
+void scratch_free(CountScratch *sc, cudaStream_t s) {
+    dfree(sc->heavy, s);
+    dfree(sc->light_mask, s);
+    dfree(sc->in_cnt, s);
+    dfree(sc->in_off, s);
+    dfree(sc->in_work, s);
+    dfree(sc->out_work, s);
+    dfree(sc->in_list, s);
+    *sc = CountScratch();
 }
 
 int device_sm_count(int device) {
@@ -281,7 +300,7 @@ int tc_ctx_create(int device, tc_ctx **out) {
     c->sm_count = device_sm_count(device);
     c->tuning.warp_max_deg = 128;
     c->tuning.light_max_work = 32768;
-    c->tuning.unit_work = 65536;
+    c->tuning.unit_work = 262144;
     c->tuning.long_list = 16;
     c->tuning.blocks_per_sm = 0;
     int st = TC_OK;
@@ -462,8 +481,7 @@ int tc_graph_destroy(tc_graph *g) {
     }
     dfree(g->d_desc, s);
     dfree(g->d_work, s);
-    dfree(g->d_heavy, s);
-    dfree(g->d_mask, s);
+    scratch_free(&g->sc, s);
     tc_ctx *ctx = g->ctx;
     delete g;
     ctx_release(ctx);
@@ -485,7 +503,7 @@ int tc_count(tc_ctx *ctx, tc_graph *g, uint64_t *out, tc_count_stats *stats) {
     TC_CUDA(cudaEventRecord(ctx->ev[2], s));
     TC_CUDA(cudaStreamSynchronize(s));
     const CountWork *w = (const CountWork *)ctx->h_pinned;
-    if (w->error) return set_error(TC_E_STATE, "heavy-unit list overflow (tuning changed under a graph?)");
+    if (w->error) return set_error(TC_E_STATE, "heavy-unit list overflow");
     *out = *(const unsigned long long *)(w + 1);
     if (stats) {
         TC_CUDA(cudaEventElapsedTime(&stats->count_ms, ctx->ev[0], ctx->ev[1]));
@@ -549,12 +567,11 @@ struct tc_batch {
     int n = 0;
     std::vector<tc_graph *> graphs;
     GraphDesc *d_desc = nullptr;
-    HeavyEntry *d_heavy = nullptr;
-    int64_t heavy_cap = 0;
-    uint32_t *d_mask = nullptr;
+    CountScratch sc{};
     CountWork *d_work = nullptr;  // followed by n results
     unsigned long long *h_out = nullptr;  // pinned: CountWork + n results
     int64_t total_chunks = 0;
+    int64_t total_vertices = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -568,8 +585,7 @@ int tc_batch_destroy(tc_batch *b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     dfree(b->d_desc, s);
-    dfree(b->d_heavy, s);
-    dfree(b->d_mask, s);
+    scratch_free(&b->sc, s);
     dfree(b->d_work, s);
     if (b->h_out) cudaFreeHost(b->h_out);
     tc_ctx *ctx = b->ctx;
@@ -587,7 +603,7 @@ int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out)
     b->n = n;
     cudaStream_t s = ctx->stream;
     std::vector<GraphDesc> desc((size_t)n);
-    int64_t chunks = 0, cap = 0;
+    int64_t chunks = 0, cap = 0, vtot = 0, etot = 0;
     for (int i = 0; i < n; ++i) {
         tc_graph *g = graphs[i];
         if (!g || g->ctx != ctx) {
@@ -595,19 +611,23 @@ int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out)
             return set_error(TC_E_INVALID, "graph %d is null or belongs to another context", i);
         }
         b->graphs.push_back(g);
+        memset(&desc[i], 0, sizeof(GraphDesc));
         desc[i].rp = g->rp;
         desc[i].col = g->col;
+        desc[i].n_rows = g->n_rows;
         desc[i].n_roots = g->n_roots;
         desc[i].chunk_base = chunks;
+        desc[i].vbase = vtot;
         desc[i].per_root = nullptr;
-        chunks += (g->n_roots + 31) / 32;
-        cap += std::min(g->n_roots, g->nnz / 2) + 1;
+        chunks += (g->n_rows + 31) / 32;
+        vtot += g->n_rows + 1;
+        etot += g->nnz;
+        cap += std::min(g->n_rows, g->nnz) + 1;
     }
     b->total_chunks = chunks;
-    b->heavy_cap = cap;
+    b->total_vertices = vtot;
     int st = dalloc((void **)&b->d_desc, sizeof(GraphDesc) * (size_t)n, s);
-    if (st == TC_OK) st = dalloc((void **)&b->d_heavy, sizeof(HeavyEntry) * (size_t)cap, s);
-    if (st == TC_OK) st = dalloc((void **)&b->d_mask, sizeof(uint32_t) * (size_t)(chunks + 1), s);
+    if (st == TC_OK) st = scratch_alloc(&b->sc, vtot, chunks, etot, cap, s);
     if (st == TC_OK) st = dalloc((void **)&b->d_work, sizeof(CountWork) + sizeof(unsigned long long) * (size_t)n, s);
     if (st == TC_OK && cudaMallocHost(&b->h_out, sizeof(CountWork) + sizeof(unsigned long long) * (size_t)n) != cudaSuccess)
         st = set_error(TC_E_NOMEM, "pinned result buffer");
@@ -619,8 +639,8 @@ int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out)
     if (st == TC_OK && cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         st = set_error(TC_E_CUDA, "stream capture could not start");
     if (st == TC_OK) {
-        int ls = launch_count(b->d_desc, n, chunks, b->d_heavy, cap, b->d_mask, b->d_work,
-                              (unsigned long long *)(b->d_work + 1), ctx->tuned, s, nullptr);
+        int ls = launch_count(b->d_desc, n, chunks, vtot, b->sc, b->d_work, (unsigned long long *)(b->d_work + 1),
+                              false, ctx->tuned, s, nullptr);
         cudaError_t e = cudaStreamEndCapture(s, &b->graph);
         if (ls != TC_OK) st = ls;
         else if (e != cudaSuccess) st = cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);

@@ -4,35 +4,51 @@
 // reference's per-block g_sum[u] (src/WithoutPartition/ShareKernelTCV62_update_v1.cu:43-191,
 // src/WithPartition/without_sorting_tc.cu:57-219), summed over roots as the
 // reference's cub::DeviceReduce::Sum does (ShareKernelTCV62_update_v1.cu:271-277).
+// Every triangle u -> v -> w (u -> w) is found once, at its oriented edge u -> v
+// as the hit w of the intersection N+(u) n N+(v).
 //
-// The reference runs one 128-thread block per root, stages N+(u) in 128-entry
-// shared tiles and binary-searches every x in N+(v) against each tile, one
-// v at a time, so most threads idle on the short lists of a power-law graph.
-// Here the same set of probes (one per oriented wedge u->v->x) is organised
-// for the GB300 as follows:
+// The reference runs one 128-thread block per root and binary-searches each x
+// of N+(v) against 128-entry shared tiles of N+(u).  Here the intersection of
+// each oriented edge u -> v is done from its cheaper side:
 //
-//  * classify (one warp per 32 roots): the warp computes, per root, d+(u) and
-//    the work w(u) = sum_{v in N+(u)} d+(v).  Light roots (d+(u) <= warp_max
-//    and w(u) <= light_max_work) are marked in a 32-bit mask per chunk; heavy
-//    roots become (#tiles x #slices) block units, #slices ~ w(u) / unit_work,
-//    appended with one packed 64-bit atomic so entries stay sorted by unit.
-//  * count (persistent grid, SMs x occupancy blocks):
-//      phase A -- blocks pull heavy units from a global cursor.  A unit builds
-//        an open-addressing hash (load factor <= 1/4) of one tile of N+(u) in
-//        shared memory; the block's warps pull 32-neighbour chunks of the
-//        unit's slice from a shared cursor and probe their wedges;
-//      phase B -- each warp pulls 32-root chunks and counts the light roots
-//        of the chunk with a per-warp shared hash of N+(u).
-//    Probing a chunk of 32 out-neighbours: lists N+(v) with d+(v) >= long_list
-//    are streamed by the whole warp, four coalesced loads in flight per lane;
-//    the shorter lists are flattened across the lanes (warp scan of d+(v),
-//    one probe per lane per step), so lanes stay busy on short lists too.
-//  * totals: per-lane u64 accumulators, warp-reduced and added with one
-//    atomic per warp per graph change.  Integer addition is associative, so
-//    the count is exact and independent of the schedule.
+//   root-centric   (d+(v) <= d+(u)): stream N+(v) through a hash of N+(u);
+//   middle-centric (d+(u) <  d+(v)): stream N+(u) through a hash of N+(v).
 //
-// The same two kernels serve the plain path (one graph per launch) and the
-// batched path (a descriptor table of many graphs or halo parts, one launch).
+// so the probes total sum_{u->v} min(d+(u), d+(v)) instead of the reference's
+// sum d+(v) (0.43x on R-MAT scale 21).  Each vertex x gets one task: a hash of
+// N+(x) and a list of partners whose lists are streamed through it -- its
+// out-neighbours v with d+(v) <= d+(x) (when x is a root) and its in-neighbours
+// u with d+(u) < d+(x) (u a root).  The in-neighbour lists are a transpose of
+// the middle-centric edges built on the device for every count.
+//
+// Launch sequence (one CUDA-graph-capturable chain, plain or batched):
+//   in_count   one warp per 32 rows: per root u, per v in N+(u), count the
+//              middle-centric in-edges of v and their work; the root-centric
+//              work of u
+//   scan       in-edge offsets
+//   transpose  per root u, scatter the middle-centric edges into the in-lists;
+//              classify each vertex x by d+(x) and its work w(x): light tasks
+//              (d+(x) <= warp_max, w(x) <= light_max_work) are marked in a
+//              32-bit mask per chunk; heavy ones become (#tiles x #slices)
+//              block units, appended with one packed 64-bit atomic so entries
+//              stay sorted by unit
+//   count      persistent grid (SMs x occupancy blocks):
+//                phase A -- blocks pull heavy units from a global cursor; a
+//                  unit hashes one tile of N+(x) (load factor <= 1/4) in shared
+//                  memory and its warps pull 4-partner chunks of the unit's
+//                  slice from a shared cursor;
+//                phase B -- each warp pulls 32-row chunks and runs the light
+//                  tasks of the chunk with a per-warp shared hash.
+//              Streaming a chunk of partners: lists with length >= long_list are
+//              read by the whole warp, four coalesced loads in flight per lane;
+//              shorter lists are flattened across the lanes (warp scan of the
+//              lengths, one probe per lane per step).
+//   totals     per-lane u64 accumulators, warp-reduced, one atomic per warp per
+//              graph change; integer addition is associative, so the count is
+//              exact and independent of the schedule.
+//
+// The same kernels serve the plain path (one graph per launch) and the batched
+// path (a descriptor table of many graphs or halo parts, one launch each).
 #include <algorithm>
 #include <cstdio>
 
@@ -46,6 +62,7 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kEmpty = -1;
 constexpr int kThreads = 256;
 constexpr int kWarpsPerBlock = kThreads / kWarp;
+constexpr int kHeavyChunk = 4;  // partners per warp grab inside a heavy unit
 
 __device__ __forceinline__ uint32_t hash_slot(int x, int shift) { return ((uint32_t)x * 0x9E3779B1u) >> shift; }
 
@@ -82,66 +99,6 @@ __device__ __forceinline__ void table_clear(int *tab, uint32_t mask, int tid, in
     for (int i = tid; i <= (int)mask; i += nthreads) tab[i] = kEmpty;
 }
 
-// Probes every wedge u->v->x for v = nbr[j], j in [j0, j1) (at most 32
-// neighbours), x in N+(v), against the hash of N+(u) (or of a tile of it).
-// Returns this lane's hit count.
-__device__ __forceinline__ uint32_t probe_chunk(const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
-                                                const int32_t *__restrict__ nbr, int j0, int j1, const int *tab,
-                                                uint32_t mask, int shift, int long_list, int lane) {
-    uint32_t hits = 0;
-    const int j = j0 + lane;
-    int s2 = 0, len = 0;
-    if (j < j1) {
-        const int v = __ldg(nbr + j);
-        s2 = __ldg(rp + v);
-        len = __ldg(rp + v + 1) - s2;
-    }
-    // long lists: the whole warp streams one list, four loads in flight per lane
-    unsigned longm = __ballot_sync(kFull, len >= long_list);
-    while (longm) {
-        const int k = __ffs(longm) - 1;
-        longm &= longm - 1u;
-        const int ls = __shfl_sync(kFull, s2, k);
-        const int ll = __shfl_sync(kFull, len, k);
-        const int32_t *__restrict__ p = col + ls;
-        for (int base = 0; base < ll; base += 4 * kWarp) {
-            int x[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int t = base + i * kWarp + lane;
-                x[i] = t < ll ? __ldg(p + t) : -1;
-            }
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-                if (x[i] >= 0) hits += table_probe(tab, mask, shift, x[i]);
-        }
-    }
-    // short lists: flattened across the lanes
-    if (len >= long_list) len = 0;
-    int incl = len;
-#pragma unroll
-    for (int o = 1; o < kWarp; o <<= 1) {
-        const int t = __shfl_up_sync(kFull, incl, o);
-        if (lane >= o) incl += t;
-    }
-    const int excl = incl - len;
-    const int total = __shfl_sync(kFull, incl, kWarp - 1);
-    for (int base = 0; base < total; base += kWarp) {
-        const int t = base + lane;
-        // largest lane k with excl_k <= t (excl is non-decreasing)
-        int seg = 0;
-#pragma unroll
-        for (int step = 16; step >= 1; step >>= 1) {
-            const int ex = __shfl_sync(kFull, excl, seg + step);
-            if (ex <= t) seg += step;
-        }
-        const int ex_seg = __shfl_sync(kFull, excl, seg);
-        const int s_seg = __shfl_sync(kFull, s2, seg);
-        if (t < total) hits += table_probe(tab, mask, shift, __ldg(col + s_seg + (t - ex_seg)));
-    }
-    return hits;
-}
-
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
@@ -166,7 +123,12 @@ struct KParams {
     int64_t heavy_cap;
     CountWork *work;
     unsigned long long *results;
-    uint32_t *light_mask;  // one word per 32-root chunk
+    uint32_t *light_mask;  // one word per 32-row chunk
+    int32_t *in_cnt;       // per vertex (pooled): middle-centric in-edges, consumed by the transpose
+    int32_t *in_off;       // per vertex (pooled) + 1: exclusive scan of in_cnt
+    unsigned long long *in_work;   // per vertex: sum of d+(u) over its in-partners u
+    unsigned long long *out_work;  // per vertex: sum of d+(v) over its out-partners v
+    int32_t *in_list;      // in-partner lists, in_off-indexed
     int warp_max;
     int log_warp_slots;
     int light_max_work;
@@ -175,50 +137,200 @@ struct KParams {
     int long_list;
 };
 
-__global__ void __launch_bounds__(kThreads) classify_kernel(KParams P, HeavyEntry *heavy) {
+// Where the partner p_j of task x lives and whose root it credits.
+struct Task {
+    const int32_t *out_nbr;  // col + rp[x]
+    const int32_t *in_nbr;   // in_list + in_off[x]
+    int n_out;               // d+(x) if x is a root, else 0
+    int dx;                  // d+(x)
+    int x;
+};
+
+// Streams the lists of partners [j0, j1) of task T (at most 32 partners)
+// through the hash of N+(x) (or of a tile of it).  Partners j < n_out are
+// out-neighbours v of x, skipped unless d+(v) <= d+(x); the others are
+// in-neighbours u.  Returns this lane's hit count; with per_root set, hits are
+// also credited to their root (x for out-partners, u for in-partners).
+template <bool kPerRoot>
+__device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
+                                                   const Task &T, int j0, int j1, const int *tab, uint32_t mask,
+                                                   int shift, int long_list, int lane,
+                                                   unsigned long long *__restrict__ per_root) {
+    uint32_t hits = 0;
+    const int j = j0 + lane;
+    int s2 = 0, len = 0, owner = T.x;
+    if (j < j1) {
+        int p;
+        if (j < T.n_out) {
+            p = __ldg(T.out_nbr + j);
+        } else {
+            p = __ldg(T.in_nbr + (j - T.n_out));
+            owner = p;
+        }
+        s2 = __ldg(rp + p);
+        len = __ldg(rp + p + 1) - s2;
+        if (j < T.n_out && len > T.dx) len = 0;  // middle-centric edge: done from p's side
+    }
+    // long lists: the whole warp streams one list, four loads in flight per lane
+    unsigned longm = __ballot_sync(kFull, len >= long_list && len > 0);
+    while (longm) {
+        const int k = __ffs(longm) - 1;
+        longm &= longm - 1u;
+        const int ls = __shfl_sync(kFull, s2, k);
+        const int ll = __shfl_sync(kFull, len, k);
+        const int32_t *__restrict__ p = col + ls;
+        uint32_t h = 0;
+        for (int base = 0; base < ll; base += 4 * kWarp) {
+            int x[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int t = base + i * kWarp + lane;
+                x[i] = t < ll ? __ldg(p + t) : -1;
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (x[i] >= 0) h += table_probe(tab, mask, shift, x[i]);
+        }
+        hits += h;
+        if (kPerRoot) {
+            const unsigned long long s = warp_sum_u64(h);
+            const int ow = __shfl_sync(kFull, owner, k);
+            if (lane == 0 && s) atomicAdd(per_root + ow, s);
+        }
+    }
+    // short lists: flattened across the lanes
+    if (len >= long_list) len = 0;
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < kWarp; o <<= 1) {
+        const int t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const int excl = incl - len;
+    const int total = __shfl_sync(kFull, incl, kWarp - 1);
+    for (int base = 0; base < total; base += kWarp) {
+        const int t = base + lane;
+        // largest lane k with excl_k <= t (excl is non-decreasing)
+        int seg = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int ex = __shfl_sync(kFull, excl, seg + step);
+            if (ex <= t) seg += step;
+        }
+        const int ex_seg = __shfl_sync(kFull, excl, seg);
+        const int s_seg = __shfl_sync(kFull, s2, seg);
+        const int own = kPerRoot ? __shfl_sync(kFull, owner, seg) : 0;
+        if (t < total) {
+            const uint32_t h = table_probe(tab, mask, shift, __ldg(col + s_seg + (t - ex_seg)));
+            hits += h;
+            if (kPerRoot && h) atomicAdd(per_root + own, 1ull);
+        }
+    }
+    return hits;
+}
+
+// in_count: per root u of a 32-row chunk, per v in N+(u): middle-centric edges
+// (d+(u) < d+(v)) add one in-edge and d+(u) of work to v; the others add d+(v)
+// to u's root-centric work.
+__global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
     const int lane = threadIdx.x & (kWarp - 1);
     const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
     const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / kWarp;
     for (int64_t c = gwarp; c < P.total_chunks; c += nwarps) {
         const int g = find_graph(P.gd, P.n_graphs, c);
-        const int32_t *__restrict__ rp = P.gd[g].rp;
-        const int32_t *__restrict__ col = P.gd[g].col;
-        const int64_t u0 = (c - P.gd[g].chunk_base) * kWarp;
+        const GraphDesc &G = P.gd[g];
+        const int32_t *__restrict__ rp = G.rp;
+        const int32_t *__restrict__ col = G.col;
+        const int64_t x0 = (c - G.chunk_base) * kWarp;
         int rs = 0, d = 0;
-        if (u0 + lane < P.gd[g].n_roots) {
-            rs = __ldg(rp + u0 + lane);
-            d = __ldg(rp + u0 + lane + 1) - rs;
+        if (x0 + lane < G.n_roots) {
+            rs = __ldg(rp + x0 + lane);
+            d = __ldg(rp + x0 + lane + 1) - rs;
         }
-        uint32_t light = 0;
-        unsigned todo = __ballot_sync(kFull, d >= 2);
+        unsigned todo = __ballot_sync(kFull, d >= 1);
         while (todo) {
             const int k = __ffs(todo) - 1;
             todo &= todo - 1u;
             const int rrs = __shfl_sync(kFull, rs, k);
             const int rd = __shfl_sync(kFull, d, k);
-            unsigned long long w = 0;
+            unsigned long long ow = 0;
             for (int i = lane; i < rd; i += kWarp) {
                 const int v = __ldg(col + rrs + i);
-                w += (unsigned long long)(__ldg(rp + v + 1) - __ldg(rp + v));
+                const int dv = __ldg(rp + v + 1) - __ldg(rp + v);
+                if (rd < dv) {
+                    atomicAdd(P.in_cnt + G.vbase + v, 1);
+                    atomicAdd(P.in_work + G.vbase + v, (unsigned long long)rd);
+                } else {
+                    ow += (unsigned long long)dv;
+                }
             }
-            w = warp_sum_u64(w);
-            if (w == 0) continue;
-            if (rd <= P.warp_max && w <= (unsigned long long)P.light_max_work) {
-                light |= 1u << k;
-                continue;
+            ow = warp_sum_u64(ow);
+            if (lane == 0) P.out_work[G.vbase + x0 + k] = ow;
+        }
+    }
+}
+
+// transpose + classify: scatter the chunk's middle-centric edges into the
+// in-lists, then classify each row of the chunk as a light task, a heavy task
+// (block units) or no work.
+__global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P, HeavyEntry *heavy) {
+    const int lane = threadIdx.x & (kWarp - 1);
+    const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / kWarp;
+    for (int64_t c = gwarp; c < P.total_chunks; c += nwarps) {
+        const int g = find_graph(P.gd, P.n_graphs, c);
+        const GraphDesc &G = P.gd[g];
+        const int32_t *__restrict__ rp = G.rp;
+        const int32_t *__restrict__ col = G.col;
+        const int64_t x0 = (c - G.chunk_base) * kWarp;
+        const int64_t x = x0 + lane;
+        int rs = 0, d = 0, nin = 0;
+        unsigned long long w = 0;
+        if (x < G.n_rows) {
+            rs = __ldg(rp + x);
+            d = __ldg(rp + x + 1) - rs;
+            nin = P.in_off[G.vbase + x + 1] - P.in_off[G.vbase + x];
+            w = P.out_work[G.vbase + x] + P.in_work[G.vbase + x];
+        }
+        // scatter the middle-centric out-edges of the chunk's roots
+        unsigned todo = __ballot_sync(kFull, d >= 1 && x < G.n_roots);
+        while (todo) {
+            const int k = __ffs(todo) - 1;
+            todo &= todo - 1u;
+            const int rrs = __shfl_sync(kFull, rs, k);
+            const int rd = __shfl_sync(kFull, d, k);
+            for (int i = lane; i < rd; i += kWarp) {
+                const int v = __ldg(col + rrs + i);
+                const int dv = __ldg(rp + v + 1) - __ldg(rp + v);
+                if (rd < dv) {
+                    const int pos = atomicSub(P.in_cnt + G.vbase + v, 1) - 1;
+                    P.in_list[P.in_off[G.vbase + v] + pos] = (int32_t)(x0 + k);
+                }
             }
-            if (lane == 0) {
-                const int max_slices = (rd + kWarp - 1) / kWarp;
+        }
+        // classify
+        const bool has = w > 0 && d >= 1;
+        const bool light = has && d <= P.warp_max && w <= (unsigned long long)P.light_max_work;
+        const bool hv = has && !light;
+        const uint32_t lm = __ballot_sync(kFull, light);
+        if (lane == 0) P.light_mask[c] = lm;
+        unsigned hm = __ballot_sync(kFull, hv);
+        while (hm) {
+            const int k = __ffs(hm) - 1;
+            hm &= hm - 1u;
+            if (lane == k) {
+                const int n_part = (x < G.n_roots ? d : 0) + nin;
+                const int max_slices = max(1, (n_part + kHeavyChunk - 1) / kHeavyChunk);
                 int ns = (int)min((w + (unsigned long long)P.unit_work - 1) / (unsigned long long)P.unit_work,
                                   (unsigned long long)max_slices);
                 ns = max(ns, 1);
-                const unsigned units = (unsigned)((rd + P.tile - 1) / P.tile) * (unsigned)ns;
+                const unsigned units = (unsigned)((d + P.tile - 1) / P.tile) * (unsigned)ns;
                 const unsigned long long base = atomicAdd(&P.work->heavy_packed, (1ull << 32) | units);
                 const unsigned long long idx = base >> 32;
                 if ((int64_t)idx < P.heavy_cap) {
                     HeavyEntry e;
                     e.g = g;
-                    e.u = (int32_t)(u0 + k);
+                    e.u = (int32_t)x;
                     e.unit_base = (int32_t)(unsigned)base;
                     e.n_slices = ns;
                     heavy[idx] = e;
@@ -227,13 +339,14 @@ __global__ void __launch_bounds__(kThreads) classify_kernel(KParams P, HeavyEntr
                 }
             }
         }
-        if (lane == 0) P.light_mask[c] = light;
     }
 }
 
+template <bool kPerRoot>
 __global__ void __launch_bounds__(kThreads) count_kernel(KParams P) {
     extern __shared__ int smem[];
     __shared__ unsigned s_unit;
+    __shared__ int s_entry;
     __shared__ int s_chunk;
     const int lane = threadIdx.x & (kWarp - 1);
     const int warp = threadIdx.x / kWarp;
@@ -255,63 +368,85 @@ __global__ void __launch_bounds__(kThreads) count_kernel(KParams P) {
     // ---- phase A: heavy units, one block each ----
     int cached_entry = -1, cached_tile = -1;
     for (;;) {
-        if (threadIdx.x == 0) {
-            s_unit = atomicAdd(&P.work->heavy_cursor, 1u);
-            s_chunk = 0;
+        if (warp == 0) {
+            unsigned unit = 0;
+            if (lane == 0) unit = atomicAdd(&P.work->heavy_cursor, 1u);
+            unit = __shfl_sync(kFull, unit, 0);
+            int e = -1;
+            if (unit < n_units && n_entries > 0) {
+                // last entry with unit_base <= unit (entries ascend; entry 0 starts at unit 0):
+                // 32-ary search, one dependent load per round
+                int lo = 0, hi = (int)n_entries;
+                while (hi - lo > kWarp) {
+                    const int step = (hi - lo + kWarp - 1) / kWarp;
+                    const int idx = lo + lane * step;
+                    const bool le = idx < hi && (unsigned)P.heavy[idx].unit_base <= unit;
+                    const unsigned m = __ballot_sync(kFull, le);
+                    lo += (31 - __clz(m)) * step;
+                    hi = min(hi, lo + step);
+                }
+                const bool le = lo + lane < hi && (unsigned)P.heavy[lo + lane].unit_base <= unit;
+                e = lo + 31 - __clz(__ballot_sync(kFull, le));
+            }
+            if (lane == 0) {
+                s_unit = unit;
+                s_entry = e;
+                s_chunk = 0;
+            }
         }
         __syncthreads();
         const unsigned unit = s_unit;
-        if (unit >= n_units || n_entries == 0) break;
-        int lo = 0, hi = (int)n_entries - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if ((unsigned)P.heavy[mid].unit_base <= unit) lo = mid;
-            else hi = mid - 1;
-        }
-        const HeavyEntry e = P.heavy[lo];
+        const int ei = s_entry;
+        if (ei < 0) break;
+        const HeavyEntry e = P.heavy[ei];
         const GraphDesc &G = P.gd[e.g];
         const int32_t *__restrict__ rp = G.rp;
         const int32_t *__restrict__ col = G.col;
+        Task T;
         const int rs = __ldg(rp + e.u);
-        const int d = __ldg(rp + e.u + 1) - rs;
+        T.dx = __ldg(rp + e.u + 1) - rs;
+        T.x = e.u;
+        T.n_out = e.u < G.n_roots ? T.dx : 0;
+        T.out_nbr = col + rs;
+        const int in0 = P.in_off[G.vbase + e.u];
+        T.in_nbr = P.in_list + in0;
+        const int n_part = T.n_out + (P.in_off[G.vbase + e.u + 1] - in0);
         const int ns = e.n_slices;
         const int k = (int)(unit - (unsigned)e.unit_base);
         const int ti = k / ns, si = k - ti * ns;
         const int t0 = ti * P.tile;
-        const int tl = min(d - t0, P.tile);
+        const int tl = min(T.dx - t0, P.tile);
         const int lg = table_log_slots(tl);
         const uint32_t mask = (1u << lg) - 1u;
         const int shift = 32 - lg;
-        if (lo != cached_entry || ti != cached_tile) {
+        if (ei != cached_entry || ti != cached_tile) {
             table_clear(smem, mask, threadIdx.x, kThreads);
             __syncthreads();
             for (int i = threadIdx.x; i < tl; i += kThreads) table_insert(smem, mask, shift, __ldg(col + rs + t0 + i));
-            cached_entry = lo;
+            cached_entry = ei;
             cached_tile = ti;
         }
         __syncthreads();
-        const int per = (d + ns - 1) / ns;
-        const int j0 = si * per, j1 = min(d, j0 + per);
+        const int per = (n_part + ns - 1) / ns;
+        const int j0 = si * per, j1 = min(n_part, j0 + per);
         uint32_t hits = 0;
         for (;;) {
             int c = 0;
             if (lane == 0) c = atomicAdd(&s_chunk, 1);
             c = __shfl_sync(kFull, c, 0);
-            const int jb = j0 + c * kWarp;
+            const int jb = j0 + c * kHeavyChunk;
             if (jb >= j1) break;
-            hits += probe_chunk(rp, col, col + rs, jb, min(jb + kWarp, j1), smem, mask, shift, P.long_list, lane);
+            hits += probe_partners<kPerRoot>(rp, col, T, jb, min(jb + kHeavyChunk, j1), smem, mask, shift, P.long_list,
+                                             lane, G.per_root);
         }
-        if (G.per_root) {
-            const unsigned long long s = warp_sum_u64(hits);
-            if (lane == 0 && s) atomicAdd(G.per_root + e.u, s);
-        } else {
+        if (!kPerRoot) {
             if (e.g != cur_g) flush(e.g);
             acc += hits;
         }
         __syncthreads();
     }
 
-    // ---- phase B: light roots, one warp each ----
+    // ---- phase B: light tasks, one warp each ----
     int *wtab = smem + warp * (1 << P.log_warp_slots);
     for (;;) {
         unsigned c = 0;
@@ -324,38 +459,43 @@ __global__ void __launch_bounds__(kThreads) count_kernel(KParams P) {
         const GraphDesc &G = P.gd[g];
         const int32_t *__restrict__ rp = G.rp;
         const int32_t *__restrict__ col = G.col;
-        if (g != cur_g && !G.per_root) flush(g);
-        const int64_t u0 = ((int64_t)c - G.chunk_base) * kWarp;
-        int rs = 0, d = 0;
+        if (!kPerRoot && g != cur_g) flush(g);
+        const int64_t x0 = ((int64_t)c - G.chunk_base) * kWarp;
+        int rs = 0, d = 0, i0 = 0, i1 = 0;
         if ((todo >> lane) & 1u) {
-            rs = __ldg(rp + u0 + lane);
-            d = __ldg(rp + u0 + lane + 1) - rs;
+            rs = __ldg(rp + x0 + lane);
+            d = __ldg(rp + x0 + lane + 1) - rs;
+            i0 = P.in_off[G.vbase + x0 + lane];
+            i1 = P.in_off[G.vbase + x0 + lane + 1];
         }
         while (todo) {
             const int k = __ffs(todo) - 1;
             todo &= todo - 1u;
+            Task T;
             const int rrs = __shfl_sync(kFull, rs, k);
-            const int rd = __shfl_sync(kFull, d, k);
-            const int lg = table_log_slots(rd);
+            T.dx = __shfl_sync(kFull, d, k);
+            T.x = (int)(x0 + k);
+            T.n_out = T.x < G.n_roots ? T.dx : 0;
+            T.out_nbr = col + rrs;
+            const int ri0 = __shfl_sync(kFull, i0, k);
+            T.in_nbr = P.in_list + ri0;
+            const int n_part = T.n_out + (__shfl_sync(kFull, i1, k) - ri0);
+            const int lg = table_log_slots(T.dx);
             const uint32_t mask = (1u << lg) - 1u;
             const int shift = 32 - lg;
             table_clear(wtab, mask, lane, kWarp);
             __syncwarp();
-            for (int i = lane; i < rd; i += kWarp) table_insert(wtab, mask, shift, __ldg(col + rrs + i));
+            for (int i = lane; i < T.dx; i += kWarp) table_insert(wtab, mask, shift, __ldg(col + rrs + i));
             __syncwarp();
             uint32_t hits = 0;
-            for (int jb = 0; jb < rd; jb += kWarp)
-                hits += probe_chunk(rp, col, col + rrs, jb, min(jb + kWarp, rd), wtab, mask, shift, P.long_list, lane);
+            for (int jb = 0; jb < n_part; jb += kWarp)
+                hits += probe_partners<kPerRoot>(rp, col, T, jb, min(jb + kWarp, n_part), wtab, mask, shift,
+                                                 P.long_list, lane, G.per_root);
             __syncwarp();
-            if (G.per_root) {
-                const unsigned long long s = warp_sum_u64(hits);
-                if (lane == 0) G.per_root[u0 + k] = s;
-            } else {
-                acc += hits;
-            }
+            if (!kPerRoot) acc += hits;
         }
     }
-    flush(-1);
+    if (!kPerRoot) flush(-1);
 }
 
 int pow2_floor_log(int x) {
@@ -378,14 +518,15 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     r.log_block_slots = pow2_floor_log(block_slots);
     r.tile = block_slots / 4;
     r.light_max_work = t.light_max_work > 0 ? t.light_max_work : 32768;
-    r.unit_work = t.unit_work > 0 ? t.unit_work : 65536;
+    r.unit_work = t.unit_work > 0 ? t.unit_work : 262144;
     r.long_list = t.long_list >= 0 ? t.long_list : 16;
     if (r.long_list > 4096) return set_error(TC_E_INVALID, "long_list must be <= 4096, got %d", r.long_list);
     r.threads = kThreads;
     r.smem = (size_t)block_slots * sizeof(int);
-    TC_CUDA(cudaFuncSetAttribute(count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
+    TC_CUDA(cudaFuncSetAttribute(count_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
+    TC_CUDA(cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
     int occ = 0;
-    TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, count_kernel, kThreads, r.smem));
+    TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, count_kernel<false>, kThreads, r.smem));
     if (occ < 1) return set_error(TC_E_INVALID, "count kernel does not fit on an SM with %zu B shared memory", r.smem);
     const int bps = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, occ) : occ;
     r.blocks = sm_count * bps;
@@ -393,18 +534,23 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     return TC_OK;
 }
 
-int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, HeavyEntry *heavy, int64_t heavy_cap,
-                 uint32_t *light_mask, CountWork *work, unsigned long long *results, const Tuned &tn, cudaStream_t s,
-                 int *launches) {
+int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, int64_t total_vertices,
+                 const CountScratch &sc, CountWork *work, unsigned long long *results, bool per_root, const Tuned &tn,
+                 cudaStream_t s, int *launches) {
     KParams P;
     P.gd = d_desc;
     P.n_graphs = n_graphs;
     P.total_chunks = total_chunks;
-    P.heavy = heavy;
-    P.heavy_cap = heavy_cap;
+    P.heavy = sc.heavy;
+    P.heavy_cap = sc.heavy_cap;
     P.work = work;
     P.results = results;
-    P.light_mask = light_mask;
+    P.light_mask = sc.light_mask;
+    P.in_cnt = sc.in_cnt;
+    P.in_off = sc.in_off;
+    P.in_work = sc.in_work;
+    P.out_work = sc.out_work;
+    P.in_list = sc.in_list;
     P.warp_max = tn.warp_max;
     P.log_warp_slots = tn.log_warp_slots;
     P.light_max_work = tn.light_max_work;
@@ -415,13 +561,20 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, He
     TC_CUDA(cudaMemsetAsync(results, 0, sizeof(unsigned long long) * (size_t)n_graphs, s));
     int nl = 0;
     if (total_chunks > 0) {
+        TC_CUDA(cudaMemsetAsync(sc.in_cnt, 0, sizeof(int32_t) * (size_t)total_vertices, s));
+        TC_CUDA(cudaMemsetAsync(sc.in_work, 0, sizeof(unsigned long long) * (size_t)total_vertices, s));
+        TC_CUDA(cudaMemsetAsync(sc.out_work, 0, sizeof(unsigned long long) * (size_t)total_vertices, s));
         const int64_t want = (total_chunks + kWarpsPerBlock - 1) / kWarpsPerBlock;
-        const int cls_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)tn.blocks * 4));
-        classify_kernel<<<cls_blocks, kThreads, 0, s>>>(P, heavy);
+        const int aux_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)tn.blocks * 4));
+        in_count_kernel<<<aux_blocks, kThreads, 0, s>>>(P);
         TC_CUDA(cudaGetLastError());
-        count_kernel<<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        TC_TRY(scan_exclusive_i32(sc.in_cnt, sc.in_off, total_vertices, s));
+        transpose_classify_kernel<<<aux_blocks, kThreads, 0, s>>>(P, sc.heavy);
         TC_CUDA(cudaGetLastError());
-        nl = 2;
+        if (per_root) count_kernel<true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        else count_kernel<false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        TC_CUDA(cudaGetLastError());
+        nl = 3 + (total_vertices > 4096 ? 3 : 1);
     }
     if (launches) *launches = nl;
     return TC_OK;

@@ -67,14 +67,31 @@ struct DBuf {
 struct GraphDesc {
     const int32_t *rp;
     const int32_t *col;
+    int64_t n_rows;
     int64_t n_roots;
-    int64_t chunk_base;           // exclusive prefix of 32-root chunks over graphs
+    int64_t chunk_base;           // exclusive prefix of 32-row chunks over graphs
+    int64_t vbase;                // exclusive prefix of (n_rows + 1) over graphs
     unsigned long long *per_root; // optional g_sum output (zeroed by the caller)
 };
 
 struct HeavyEntry {
     int32_t g, u, unit_base, n_slices;  // units = ceil(d+(u) / tile) * n_slices
 };
+
+// Device arrays of one count launch, sized for its graphs (pooled over a batch):
+// V = sum (n_rows + 1), C = sum ceil(n_rows / 32), E = sum nnz.
+struct CountScratch {
+    HeavyEntry *heavy = nullptr;  // heavy_cap entries
+    int64_t heavy_cap = 0;
+    uint32_t *light_mask = nullptr;         // C words
+    int32_t *in_cnt = nullptr;              // V
+    int32_t *in_off = nullptr;              // V + 1
+    unsigned long long *in_work = nullptr;  // V
+    unsigned long long *out_work = nullptr; // V
+    int32_t *in_list = nullptr;             // E
+};
+int scratch_alloc(CountScratch *sc, int64_t V, int64_t C, int64_t E, int64_t heavy_cap, cudaStream_t s);
+void scratch_free(CountScratch *sc, cudaStream_t s);
 
 // Per-launch device words, zeroed by one memset before each count.
 struct CountWork {
@@ -102,10 +119,11 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out);
 
 // Enqueues classify + persistent count for n_graphs descriptors on stream s.
 // results[n_graphs] receives the per-graph totals (zeroed here).
-// light_mask holds one word per 32-root chunk (total_chunks words).
-int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, HeavyEntry *heavy, int64_t heavy_cap,
-                 uint32_t *light_mask, CountWork *work, unsigned long long *results, const Tuned &tn, cudaStream_t s,
-                 int *launches);
+// Enqueues [in_count -> scan -> transpose/classify -> count] for n_graphs
+// descriptors on stream s; total_vertices = sum (n_rows + 1).
+int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, int64_t total_vertices,
+                 const CountScratch &sc, CountWork *work, unsigned long long *results, bool per_root, const Tuned &tn,
+                 cudaStream_t s, int *launches);
 
 // ---- scans and sort (tc_scan.cu, tc_sort.cu) ----------------------------------------
 // Exclusive scan of n values into out[0..n] (out[n] = total).  out may alias in.
@@ -150,9 +168,7 @@ struct tc_graph {
     tc::GraphDesc *d_desc = nullptr;
     tc::CountWork *d_work = nullptr;
     unsigned long long *d_result = nullptr;
-    tc::HeavyEntry *d_heavy = nullptr;
-    int64_t heavy_cap = 0;
-    uint32_t *d_mask = nullptr;          // light-root mask, one word per 32 roots
+    tc::CountScratch sc{};
     tc::GraphDesc desc_on_device{};  // what d_desc holds (skip re-uploads)
     bool desc_valid = false;
 };
