@@ -144,6 +144,20 @@ TC_API int tc_count_per_root(tc_ctx *ctx, tc_graph *g, uint64_t *per_root, uint6
 TC_API int tc_count_csr_i32(tc_ctx *ctx, const int32_t *row_ptr, const int32_t *col, int64_t n_rows, int64_t nnz,
                             uint64_t *out);
 
+/* Count without allocating: for callers that may not allocate GPU memory
+ * themselves (an application that owns the device heap and forbids library
+ * cudaMalloc calls, a real-time loop, a sandboxed plugin).  No counterpart in
+ * the reference.  d_row_ptr / d_col are device arrays of an oriented CSR as in
+ * tc_graph_upload_i32 (not validated); roots are rows [0, n_roots); the count
+ * is written to the device word d_out in stream order on `stream` (a
+ * cudaStream_t, NULL for the default stream).  Scratch is one fixed ~18 MB
+ * device array inside libtc: at most 262,144 rows and 2,097,152 oriented edges
+ * (TC_E_RANGE beyond).  Calls share that array, so calls that overlap on the
+ * GPU race; the first call on a device sets up that device and should come
+ * before any stream capture. */
+TC_API int tc_count_noalloc_i32(const int32_t *d_row_ptr, const int32_t *d_col, int64_t n_rows, int64_t nnz,
+                                int64_t n_roots, uint64_t *d_out, void *stream);
+
 /* ---- batched counting: many graphs or parts, one persistent launch --------- */
 /* Replaces the sequential per-part loop of without_sorting_tc.cu:244-465 (one
  * launch + host sync per part).  A batch holds the descriptor table of its

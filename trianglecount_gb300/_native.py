@@ -67,6 +67,7 @@ _SIGS = {
     "tc_count_async": (C.c_int, [vp, vp, vp]),
     "tc_count_per_root": (C.c_int, [vp, vp, vp, P(u64)]),
     "tc_count_csr_i32": (C.c_int, [vp, vp, vp, i64, i64, P(u64)]),
+    "tc_count_noalloc_i32": (C.c_int, [vp, vp, i64, i64, i64, vp, vp]),
     "tc_batch_create": (C.c_int, [vp, P(vp), C.c_int, P(vp)]),
     "tc_batch_run": (C.c_int, [vp, vp]),
     "tc_batch_run_async": (C.c_int, [vp]),

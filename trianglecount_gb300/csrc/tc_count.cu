@@ -580,4 +580,46 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
     return TC_OK;
 }
 
+int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t total_vertices,
+                         const CountScratch &sc, int32_t *scan_tmp, int64_t scan_tmp_cap, CountWork *work,
+                         unsigned long long *results, const Tuned &tn, cudaStream_t s) {
+    KParams P;
+    P.gd = d_desc;
+    P.n_graphs = 1;
+    P.total_chunks = total_chunks;
+    P.heavy = sc.heavy;
+    P.heavy_cap = sc.heavy_cap;
+    P.work = work;
+    P.results = results;
+    P.light_mask = sc.light_mask;
+    P.in_cnt = sc.in_cnt;
+    P.in_off = sc.in_off;
+    P.in_work = sc.in_work;
+    P.out_work = sc.out_work;
+    P.in_list = sc.in_list;
+    P.warp_max = tn.warp_max;
+    P.log_warp_slots = tn.log_warp_slots;
+    P.light_max_work = tn.light_max_work;
+    P.unit_work = tn.unit_work;
+    P.tile = tn.tile;
+    P.long_list = tn.long_list;
+    TC_CUDA(cudaMemsetAsync(work, 0, sizeof(CountWork), s));
+    TC_CUDA(cudaMemsetAsync(results, 0, sizeof(unsigned long long), s));
+    if (total_chunks > 0) {
+        TC_CUDA(cudaMemsetAsync(sc.in_cnt, 0, sizeof(int32_t) * (size_t)total_vertices, s));
+        TC_CUDA(cudaMemsetAsync(sc.in_work, 0, sizeof(unsigned long long) * (size_t)total_vertices, s));
+        TC_CUDA(cudaMemsetAsync(sc.out_work, 0, sizeof(unsigned long long) * (size_t)total_vertices, s));
+        const int64_t want = (total_chunks + kWarpsPerBlock - 1) / kWarpsPerBlock;
+        const int aux_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)tn.blocks * 4));
+        in_count_kernel<<<aux_blocks, kThreads, 0, s>>>(P);
+        TC_CUDA(cudaGetLastError());
+        TC_TRY(scan_exclusive_i32_tmp(sc.in_cnt, sc.in_off, total_vertices, scan_tmp, scan_tmp_cap, s));
+        transpose_classify_kernel<<<aux_blocks, kThreads, 0, s>>>(P, sc.heavy);
+        TC_CUDA(cudaGetLastError());
+        count_kernel<false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        TC_CUDA(cudaGetLastError());
+    }
+    return TC_OK;
+}
+
 }  // namespace tc

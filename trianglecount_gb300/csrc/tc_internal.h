@@ -117,6 +117,12 @@ struct Tuned {  // resolved tc_tuning with derived table geometry
 
 int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out);
 
+// launch_count for callers that cannot allocate: the in-edge scan keeps its
+// tile sums in scan_tmp (scan_tmp_cap values); nothing is allocated.
+int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t total_vertices,
+                         const CountScratch &sc, int32_t *scan_tmp, int64_t scan_tmp_cap, CountWork *work,
+                         unsigned long long *results, const Tuned &tn, cudaStream_t s);
+
 // Enqueues classify + persistent count for n_graphs descriptors on stream s.
 // results[n_graphs] receives the per-graph totals (zeroed here).
 // Enqueues [in_count -> scan -> transpose/classify -> count] for n_graphs
@@ -131,6 +137,9 @@ int scan_exclusive_i32(const int32_t *in, int32_t *out, int64_t n, cudaStream_t 
 int scan_exclusive_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s);
 // Exclusive scan of 0/1 byte flags into int32 positions out[0..n].
 int scan_flags_u8(const uint8_t *flags, int32_t *out, int64_t n, cudaStream_t s);
+// scan_exclusive_i32 with its tile sums in caller memory (no allocation).
+int scan_exclusive_i32_tmp(const int32_t *in, int32_t *out, int64_t n, int32_t *tmp, int64_t tmp_cap,
+                           cudaStream_t s);
 // LSD radix sort of n 64-bit keys on bits [0, bits).  Result in *keys (the
 // two buffers may be swapped).  tmp must hold n keys.
 int radix_sort_u64(uint64_t **keys, uint64_t **tmp, int64_t n, int bits, cudaStream_t s);

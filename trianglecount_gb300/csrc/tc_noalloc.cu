@@ -1,0 +1,128 @@
+// tc_noalloc.cu -- triangle count that allocates no memory.
+//
+// Some callers cannot allocate GPU memory on their own: an application that
+// owns the device heap through its own allocator and forbids libraries from
+// calling cudaMalloc, a real-time loop where an allocation (and the
+// synchronisation it may imply) is not acceptable, or a sandboxed plugin whose
+// host denies allocations.  tc_count_noalloc_i32 serves them: the caller hands
+// in device pointers to the oriented CSR and to the 8-byte result, and every
+// scratch array the count needs lives in one file-scope device array of fixed
+// size (kScratchBytes below, about 18 MB), which each GPU that loads libtc
+// keeps until the process exits.
+//
+// Limits: n_rows <= kMaxRows (262,144) and nnz <= kMaxNnz (2,097,152); larger
+// graphs are rejected with TC_E_RANGE.  All calls share the one array, so two
+// calls whose work overlaps on the GPU (different streams, or different host
+// threads) race and give wrong counts; order them on one stream.  The first
+// call on a device looks up the array's device address and the kernel
+// configuration for that device (cudaGetSymbolAddress, occupancy query); make
+// that first call before any stream capture.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+#include "tc_internal.h"
+
+namespace tc {
+namespace {
+
+constexpr int64_t kMaxRows = 1 << 18;
+constexpr int64_t kMaxNnz = 1 << 21;
+constexpr int64_t kScanTmp = 4096;  // tile sums of the in-edge scan (needs 66 for kMaxRows)
+
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Byte offsets of the scratch sections (each 256-byte aligned).
+constexpr size_t kOffWork = 0;  // CountWork + 8-byte result
+constexpr size_t kOffDesc = align256(kOffWork + sizeof(CountWork) + 8);
+constexpr size_t kOffMask = align256(kOffDesc + sizeof(GraphDesc));
+constexpr size_t kOffHeavy = align256(kOffMask + sizeof(uint32_t) * (kMaxRows / 32 + 1));
+constexpr size_t kOffInCnt = align256(kOffHeavy + sizeof(HeavyEntry) * (kMaxRows + 1));
+constexpr size_t kOffInOff = align256(kOffInCnt + sizeof(int32_t) * (kMaxRows + 1));
+constexpr size_t kOffInWork = align256(kOffInOff + sizeof(int32_t) * (kMaxRows + 2));
+constexpr size_t kOffOutWork = align256(kOffInWork + sizeof(unsigned long long) * (kMaxRows + 1));
+constexpr size_t kOffInList = align256(kOffOutWork + sizeof(unsigned long long) * (kMaxRows + 1));
+constexpr size_t kOffScan = align256(kOffInList + sizeof(int32_t) * kMaxNnz);
+constexpr size_t kScratchBytes = align256(kOffScan + sizeof(int32_t) * kScanTmp);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+struct DeviceSetup {
+    bool ready = false;
+    unsigned char *scratch = nullptr;  // device address of g_noalloc_scratch
+    Tuned tuned{};
+};
+
+std::mutex g_setup_mu;
+DeviceSetup g_setup[64];
+
+// Once per device, with that device current: the array's device address and
+// the default kernel configuration.  The array's name is only a host-side
+// stand-in in host code, so kernels are given the looked-up address.
+int setup_device(int dev, DeviceSetup **out) {
+    if (dev < 0 || dev >= 64) return set_error(TC_E_NO_DEVICE, "device %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_setup_mu);
+    DeviceSetup &d = g_setup[dev];
+    if (!d.ready) {
+        void *p = nullptr;
+        TC_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        tc_tuning t{};
+        t.warp_max_deg = 128;
+        t.light_max_work = 32768;
+        t.unit_work = 262144;
+        t.long_list = 16;
+        t.blocks_per_sm = 0;
+        TC_TRY(resolve_tuning(t, device_sm_count(dev), &d.tuned));
+        d.scratch = (unsigned char *)p;
+        d.ready = true;
+    }
+    *out = &d;
+    return TC_OK;
+}
+
+}  // namespace
+}  // namespace tc
+
+using namespace tc;
+
+extern "C" int tc_count_noalloc_i32(const int32_t *d_row_ptr, const int32_t *d_col, int64_t n_rows, int64_t nnz,
+                                    int64_t n_roots, uint64_t *d_out, void *stream) {
+    if (!d_row_ptr || (nnz > 0 && !d_col) || !d_out) return set_error(TC_E_INVALID, "null device pointer");
+    if (n_rows < 0 || nnz < 0 || n_roots < 0 || n_roots > n_rows)
+        return set_error(TC_E_INVALID, "bad sizes: n_rows=%lld nnz=%lld n_roots=%lld", (long long)n_rows,
+                         (long long)nnz, (long long)n_roots);
+    if (n_rows > kMaxRows || nnz > kMaxNnz)
+        return set_error(TC_E_RANGE,
+                         "tc_count_noalloc_i32 handles at most %lld rows and %lld oriented edges (got %lld, %lld); "
+                         "use tc_count for larger graphs",
+                         (long long)kMaxRows, (long long)kMaxNnz, (long long)n_rows, (long long)nnz);
+    int dev = 0;
+    TC_CUDA(cudaGetDevice(&dev));
+    DeviceSetup *ds = nullptr;
+    TC_TRY(setup_device(dev, &ds));
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned char *base = ds->scratch;
+    CountWork *work = (CountWork *)(base + kOffWork);
+    unsigned long long *result = (unsigned long long *)(work + 1);
+    GraphDesc *desc = (GraphDesc *)(base + kOffDesc);
+    CountScratch sc;
+    sc.heavy = (HeavyEntry *)(base + kOffHeavy);
+    sc.heavy_cap = std::min(n_rows, nnz) + 1;
+    sc.light_mask = (uint32_t *)(base + kOffMask);
+    sc.in_cnt = (int32_t *)(base + kOffInCnt);
+    sc.in_off = (int32_t *)(base + kOffInOff);
+    sc.in_work = (unsigned long long *)(base + kOffInWork);
+    sc.out_work = (unsigned long long *)(base + kOffOutWork);
+    sc.in_list = (int32_t *)(base + kOffInList);
+    GraphDesc d;
+    memset(&d, 0, sizeof d);
+    d.rp = d_row_ptr;
+    d.col = d_col;
+    d.n_rows = n_rows;
+    d.n_roots = n_roots;
+    TC_CUDA(cudaMemcpyAsync(desc, &d, sizeof d, cudaMemcpyHostToDevice, s));
+    TC_TRY(launch_count_noalloc(desc, (n_rows + 31) / 32, n_rows + 1, sc, (int32_t *)(base + kOffScan), kScanTmp,
+                                work, result, ds->tuned, s));
+    TC_CUDA(cudaMemcpyAsync(d_out, result, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+    return TC_OK;
+}

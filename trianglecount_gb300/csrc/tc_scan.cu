@@ -219,7 +219,34 @@ __global__ void __launch_bounds__(kT) radix_scatter_kernel(const uint64_t *keys,
     }
 }
 
+// Same scan with the tile sums of every recursion level in tmp (tmp_cap values).
+template <class In, class Out>
+int scan_tmp_impl(const In *in, Out *out, int64_t n, Out *tmp, int64_t tmp_cap, cudaStream_t s) {
+    if (n <= 0) {
+        TC_CUDA(cudaMemsetAsync(out, 0, sizeof(Out), s));
+        return TC_OK;
+    }
+    const int64_t tiles = (n + kTile - 1) / kTile;
+    if (tiles == 1) {
+        single_tile_scan_kernel<In, Out><<<1, kT, 0, s>>>(in, n, out);
+        TC_CUDA(cudaGetLastError());
+        return TC_OK;
+    }
+    if (tiles + 1 > tmp_cap) return set_error(TC_E_RANGE, "scan temp of %lld values is too small", (long long)tmp_cap);
+    tile_reduce_kernel<In, Out><<<(unsigned)tiles, kT, 0, s>>>(in, n, tmp);
+    TC_CUDA(cudaGetLastError());
+    TC_TRY((scan_tmp_impl<Out, Out>(tmp, tmp, tiles, tmp + tiles + 1, tmp_cap - (tiles + 1), s)));
+    tile_scan_kernel<In, Out><<<(unsigned)tiles, kT, 0, s>>>(in, n, tmp, out);
+    TC_CUDA(cudaGetLastError());
+    return TC_OK;
+}
+
 }  // namespace
+
+int scan_exclusive_i32_tmp(const int32_t *in, int32_t *out, int64_t n, int32_t *tmp, int64_t tmp_cap,
+                           cudaStream_t s) {
+    return scan_tmp_impl<int32_t, int32_t>(in, out, n, tmp, tmp_cap, s);
+}
 
 int scan_exclusive_i32(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s) {
     return scan_impl<int32_t, int32_t>(in, out, n, s);
