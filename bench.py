@@ -56,7 +56,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["rmat21", "road", "rmat16", "rmat18", "rmat23"], default="rmat21")
+    ap.add_argument("--workload", choices=["rmat21", "road", "rmat16", "rmat18", "rmat23", "rmat23_parts", "batch256"],
+                    default="rmat21")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-ref-kernel", action="store_true")
     return ap.parse_args()
@@ -245,6 +246,8 @@ def run_ours(args, world, rank, local, pg):
         one_step(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
     torch.cuda.synchronize()
     count = int(d_out.item())
+    _, st0 = ctx.count(g, stats=True)
+    launches_per_count = int(st0["launches"])
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -304,11 +307,11 @@ def run_ours(args, world, rank, local, pg):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded R-MAT / grid generators)",
             "config": cfg,
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": launches_per_count * args.steps,
             "e2e": {"value": world * E / (e2e / 1000.0), "unit": UNIT, "ms_per_step": e2e,
                     "h2d_bytes_per_step": 4 * (V + 1) + 4 * E, "d2h_bytes_per_step": 8 + 8 + 24,
                     "path": "tc_count_csr_i32 (upload + validate + count + read-back)",
-                    "gpu_launches": 4 * args.steps},
+                    "gpu_launches": (launches_per_count + 2) * args.steps},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": f"{peak_src} hbm_gbs (copy, burst)",
                          "algorithmic_bytes_per_launch": B_alg,
@@ -350,13 +353,137 @@ def run_ours(args, world, rank, local, pg):
     return res
 
 
+def _timed(stream, flush, fn, steps, warmup):
+    import torch
+    ms = []
+    for i in range(warmup + steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0.record(stream)
+        fn()
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        if i >= warmup:
+            ms.append(e0.elapsed_time(e1))
+    return sum(ms) / len(ms)
+
+
+def run_parts(args, world, rank, local, pg):
+    """Partitioned halo path on R-MAT scale 23: device clean-up, orientation and
+    halo extraction for k = 2, 4, 8 seeded random parts; every part counted by
+    its own launch (host sync after each, as the reference's per-part loop)
+    versus all parts in one persistent launch (CUDA-graph replay)."""
+    import torch
+
+    import trianglecount_gb300 as tc
+    from trianglecount_gb300 import generators as gen
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    ctx = tc.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    t0 = time.perf_counter()
+    src, dst = gen.rmat(23, 16)
+    gen_s = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ug = ctx.ugraph_from_edges(src, dst)
+    clean_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    og = ctx.orient(ug)
+    orient_s = time.perf_counter() - t0
+    V, E = og.n_rows, og.nnz
+    whole = ctx.count(og)
+    whole_ms = _timed(stream, flush, lambda: ctx.count(og), args.steps, args.warmup)
+    per_k = {}
+    for k in (2, 4, 8):
+        part = gen.parts_random(V, k)
+        t0 = time.perf_counter()
+        parts = ctx.halo_extract(ug, part, k)
+        halo_s = time.perf_counter() - t0
+        plain_ms = _timed(stream, flush, lambda: ctx.count_each(parts), args.steps, args.warmup)
+        b = ctx.batch(parts)
+        out = b.run()
+        batch_ms = _timed(stream, flush, lambda: b.run(), args.steps, args.warmup)
+        assert int(out.sum()) == whole and int(ctx.count_each(parts).sum()) == whole
+        per_k[str(k)] = {"plain_per_part_ms": plain_ms, "batched_ms": batch_ms, "speedup": plain_ms / batch_ms,
+                         "parts_nnz": [p.nnz for p in parts], "parts_rows": [p.n_rows for p in parts],
+                         "halo_extract_s": halo_s, "sum_of_parts": int(out.sum())}
+        b.free()
+    ms = per_k["8"]["batched_ms"]
+    cfg = {"workload": "rmat23_ef16_halo_parts", "scale": 23, "edge_factor": 16, "V": V, "oriented_edges": E,
+           "triangles": whole, "parts": per_k, "whole_graph_plain_ms": whole_ms,
+           "host_generate_s": gen_s, "device_clean_s": clean_s, "device_orient_s": orient_s,
+           "partition": "seeded uniform random, k = 2, 4, 8",
+           "l2": "flushed before every timed step (512 MiB memset on the launching stream)"}
+    res = {"metric": METRIC, "value": world * E / (ms / 1000.0), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "int32", "data": "synthetic (seeded R-MAT scale 23)", "config": cfg}
+    ctx.close()
+    return res
+
+
+def run_batch(args, world, rank, local, pg):
+    """Uneven batch: 256 seeded ER / Chung-Lu / R-MAT graphs, one launch per
+    graph (host sync after each) versus one persistent launch for all."""
+    import torch
+
+    import oracle
+    import trianglecount_gb300 as tc
+    from trianglecount_gb300 import generators as gen
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    ctx = tc.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    specs = gen.batch_mix(256)
+    graphs, gen_s, prep_s = [], 0.0, 0.0
+    for sp in specs:
+        t0 = time.perf_counter()
+        src, dst = sp.edges()
+        gen_s += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        graphs.append(ctx.graph_from_edges(src, dst))
+        prep_s += time.perf_counter() - t0
+    E = sum(g.nnz for g in graphs)
+    each = ctx.count_each(graphs)
+    b = ctx.batch(graphs)
+    outs = b.run()
+    assert list(outs) == list(each)
+    # oracle spot check on the smallest graphs
+    small = sorted(range(len(specs)), key=lambda i: graphs[i].nnz)[:8]
+    for i in small:
+        rp, col = graphs[i].download()
+        assert oracle.count(rp, col) == int(outs[i])
+    plain_ms = _timed(stream, flush, lambda: ctx.count_each(graphs), args.steps, args.warmup)
+    batch_ms = _timed(stream, flush, lambda: b.run(), args.steps, args.warmup)
+    kinds = {k: sum(1 for s in specs if s.kind == k) for k in ("er", "chung_lu", "rmat")}
+    cfg = {"workload": "uneven_batch_256", "graphs": len(graphs), "kinds": kinds, "oriented_edges": E,
+           "triangles_total": int(outs.sum()), "plain_per_graph_ms": plain_ms, "batched_ms": batch_ms,
+           "speedup": plain_ms / batch_ms, "host_generate_s": gen_s, "device_preprocess_s": prep_s,
+           "largest_graph_edges": max(g.nnz for g in graphs), "smallest_graph_edges": min(g.nnz for g in graphs),
+           "l2": "flushed before every timed step (512 MiB memset on the launching stream)"}
+    res = {"metric": METRIC, "value": world * E / (batch_ms / 1000.0), "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": batch_ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+           "data": "synthetic (seeded ER / Chung-Lu / R-MAT mix)", "config": cfg}
+    b.free()
+    ctx.close()
+    return res
+
+
 def main():
     args = parse()
     world, rank, local, pg = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:
-        res = run_ours(args, world, rank, local, pg)
+        fn = {"rmat23_parts": run_parts, "batch256": run_batch}.get(args.workload, run_ours)
+        res = fn(args, world, rank, local, pg)
         if rank == 0:
             print(json.dumps(res), flush=True)
     if pg is not None:

@@ -201,7 +201,9 @@ TC_API int tc_graph_from_edges(tc_ctx *ctx, const int64_t *src, const int64_t *d
  * vertices (ascending) then their 1-hop halo (ascending) get local ids; the
  * oriented edges among them are kept with rows ascending; halo vertices with
  * zero in-degree are pruned until none is left.  parts_out[p] is an oriented
- * graph with n_roots = t_ver.  part[] is a host array of n_rows ints in [0,k).
+ * graph with n_roots = t_ver.  part[] is a host array of n_rows non-negative
+ * ints; a vertex with part >= k belongs to no extracted part (it can still be
+ * in a part's halo), as in the reference's loop over parts 0..k-1.
  * Replaces create_subgraph_with_halo (round_clean_subgraph.cu:357-902) with
  * the prune of Halo_creation_preprocess.py:566-589. */
 TC_API int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k, int tie,
@@ -225,6 +227,13 @@ TC_API int tc_text_write_line(const char *path, const void *values, int64_t n, i
 /* Page-locked host memory for fast transfers (cudaMallocHost). */
 TC_API int tc_host_alloc_pinned(size_t bytes, void **out);
 TC_API int tc_host_free_pinned(void *p);
+/* Edge list of a graph file in the formats the reference's preprocessing
+ * reads (Med_dataset/without_part_preprocess.py:126-177): .tsv (Graph
+ * Challenge "src dst weight"), .txt (SNAP, '#' comment lines), .mtx / .mmio
+ * (Matrix Market coordinate, 1-based, '%' comments, size line skipped); any
+ * other extension: two ids per line.  Extra columns are ignored.  *src/*dst
+ * are malloc'd by the library (release with tc_host_free). */
+TC_API int tc_read_edges(const char *path, int64_t **src, int64_t **dst, int64_t *n_edges);
 /* Binary CSR cache (.tcsr): header + int64 row_ptr + int32 col. */
 TC_API int tc_tcsr_write(const char *path, const int64_t *row_ptr, const int32_t *col, int64_t n_rows,
                          int64_t nnz, int64_t n_roots, int64_t aux);

@@ -87,6 +87,7 @@ _SIGS = {
     "tc_text_write_line": (C.c_int, [C.c_char_p, vp, i64, C.c_int, C.c_char, C.c_int]),
     "tc_host_alloc_pinned": (C.c_int, [C.c_size_t, P(vp)]),
     "tc_host_free_pinned": (C.c_int, [vp]),
+    "tc_read_edges": (C.c_int, [C.c_char_p, P(P(i64)), P(P(i64)), P(i64)]),
     "tc_tcsr_write": (C.c_int, [C.c_char_p, vp, vp, i64, i64, i64, i64]),
     "tc_tcsr_read_header": (C.c_int, [C.c_char_p, P(i64), P(i64), P(i64), P(i64)]),
     "tc_tcsr_read": (C.c_int, [C.c_char_p, vp, vp]),

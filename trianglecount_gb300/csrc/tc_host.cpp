@@ -215,6 +215,69 @@ int tc_text_write_line(const char *path, const void *values, int64_t n, int elem
     return ok ? TC_OK : set_error(TC_E_IO, "write to %s failed", path);
 }
 
+int tc_read_edges(const char *path, int64_t **src, int64_t **dst, int64_t *n_edges) {
+    if (!path || !src || !dst || !n_edges) return set_error(TC_E_INVALID, "null argument");
+    *src = *dst = nullptr;
+    *n_edges = 0;
+    std::vector<char> buf;
+    TC_TRY(read_file(path, buf));
+    const char *ext = strrchr(path, '.');
+    const bool mtx = ext && (strcmp(ext, ".mtx") == 0 || strcmp(ext, ".mmio") == 0);
+    std::vector<int64_t> s, d;
+    const char *p = buf.data(), *end = buf.data() + buf.size() - 1;
+    bool size_line_pending = mtx;
+    int64_t line_no = 0;
+    while (p < end) {
+        const char *eol = (const char *)memchr(p, '\n', (size_t)(end - p));
+        if (!eol) eol = end;
+        ++line_no;
+        const char *q = p;
+        while (q < eol && (*q == ' ' || *q == '\t' || *q == '\r')) ++q;
+        if (q < eol && *q != '#' && *q != '%') {
+            int64_t v[2];
+            int got = 0;
+            while (got < 2 && q < eol) {
+                while (q < eol && (*q == ' ' || *q == '\t' || *q == ',' || *q == '\r')) ++q;
+                if (q >= eol) break;
+                if (!isdigit((unsigned char)*q)) {
+                    return set_error(TC_E_FORMAT, "%s:%lld: expected a vertex id", path, (long long)line_no);
+                }
+                int64_t x = 0;
+                while (q < eol && isdigit((unsigned char)*q)) x = x * 10 + (*q++ - '0');
+                v[got++] = x;
+            }
+            if (got < 2) return set_error(TC_E_FORMAT, "%s:%lld: expected two vertex ids", path, (long long)line_no);
+            if (size_line_pending) {
+                size_line_pending = false;  // Matrix Market "rows cols nnz" line
+            } else if (mtx) {
+                if (v[0] < 1 || v[1] < 1) return set_error(TC_E_FORMAT, "%s:%lld: Matrix Market ids are 1-based", path,
+                                                           (long long)line_no);
+                s.push_back(v[0] - 1);
+                d.push_back(v[1] - 1);
+            } else {
+                s.push_back(v[0]);
+                d.push_back(v[1]);
+            }
+        }
+        p = eol + 1;
+    }
+    const int64_t n = (int64_t)s.size();
+    *src = (int64_t *)malloc(sizeof(int64_t) * (size_t)std::max<int64_t>(n, 1));
+    *dst = (int64_t *)malloc(sizeof(int64_t) * (size_t)std::max<int64_t>(n, 1));
+    if (!*src || !*dst) {
+        free(*src);
+        free(*dst);
+        *src = *dst = nullptr;
+        return set_error(TC_E_NOMEM, "host allocation for %lld edges", (long long)n);
+    }
+    if (n) {
+        memcpy(*src, s.data(), sizeof(int64_t) * (size_t)n);
+        memcpy(*dst, d.data(), sizeof(int64_t) * (size_t)n);
+    }
+    *n_edges = n;
+    return TC_OK;
+}
+
 int tc_tcsr_write(const char *path, const int64_t *row_ptr, const int32_t *col, int64_t n_rows, int64_t nnz,
                   int64_t n_roots, int64_t aux) {
     if (!path || !row_ptr || (nnz > 0 && !col)) return set_error(TC_E_INVALID, "null argument");

@@ -544,7 +544,7 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
     cudaStream_t s = ctx->stream;
     const int64_t V = ug->n_rows, nnz = ug->nnz;
     for (int64_t v = 0; v < V; ++v)
-        if (part[v] < 0 || part[v] >= k) return set_error(TC_E_RANGE, "part[%lld] = %d outside [0, %d)", (long long)v, part[v], k);
+        if (part[v] < 0) return set_error(TC_E_RANGE, "part[%lld] = %d is negative", (long long)v, part[v]);
     DBuf<int32_t> dpart, lidP, lidH, lid, cnt, lrp, posP, posH;
     DBuf<uint8_t> inP, inH, fP, fH;
     TC_TRY(dpart.alloc((size_t)std::max<int64_t>(V, 1), s));

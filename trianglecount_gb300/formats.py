@@ -161,6 +161,21 @@ def write_parts_output(path, V: int, E: int, parts: list) -> None:
         write_line(path, hp.col, "a")
 
 
+def read_edges(path) -> tuple[np.ndarray, np.ndarray]:
+    """Edge list of a .tsv / .txt / .mtx / .mmio graph file (int64 src, dst)."""
+    s = C.POINTER(C.c_int64)()
+    d = C.POINTER(C.c_int64)()
+    n = C.c_int64()
+    N.call("tc_read_edges", os.fsencode(path), C.byref(s), C.byref(d), C.byref(n))
+    try:
+        if n.value == 0:
+            return np.empty(0, np.int64), np.empty(0, np.int64)
+        return (np.ctypeslib.as_array(s, shape=(n.value,)).copy(), np.ctypeslib.as_array(d, shape=(n.value,)).copy())
+    finally:
+        N.lib().tc_host_free(C.cast(s, C.c_void_p))
+        N.lib().tc_host_free(C.cast(d, C.c_void_p))
+
+
 def write_tcsr(path, row_ptr: np.ndarray, col: np.ndarray, n_roots: int | None = None, aux: int = 0) -> None:
     rp = np.ascontiguousarray(row_ptr, np.int64)
     cl = np.ascontiguousarray(col, np.int32)
