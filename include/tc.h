@@ -100,6 +100,12 @@ typedef struct tc_tuning {
 } tc_tuning;
 TC_API int tc_ctx_get_tuning(tc_ctx *ctx, tc_tuning *out);
 TC_API int tc_ctx_set_tuning(tc_ctx *ctx, const tc_tuning *in);
+/* Autotuner: times the count of g under candidate thresholds (coordinate
+ * descent from the current tuning over warp_max_deg, light_max_work,
+ * unit_work, long_list; each candidate the median of `reps` counts) and sets
+ * the fastest on ctx.  best / best_ms may be NULL.  At most max_trials
+ * candidates are timed. */
+TC_API int tc_autotune(tc_ctx *ctx, tc_graph *g, int max_trials, int reps, tc_tuning *best, float *best_ms);
 
 /* ---- oriented graphs ------------------------------------------------------ */
 /* Upload an oriented CSR: n_rows rows, row_ptr[n_rows+1], col[nnz], rows
@@ -209,6 +215,46 @@ TC_API int tc_graph_from_edges(tc_ctx *ctx, const int64_t *src, const int64_t *d
 TC_API int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k, int tie,
                            tc_graph **parts_out);
 
+/* ---- serving: continuous batching over resident graphs ----------------------- */
+/* No counterpart in the reference (which runs one file per process).  A server
+ * owns two contexts on ctx's device: a prep thread admits queued requests by
+ * device-memory footprint (evicting least-recently-used idle graphs to stay
+ * within the budget) and builds their oriented CSRs on one stream, while a
+ * count thread counts every ready request in one batched launch on the other
+ * stream; requests arriving during a count are preprocessed concurrently and
+ * join the next batch.  Waits are host-side and bounded by batch_timeout_ms;
+ * a batch that exceeds it fails with TC_E_TIMEOUT and the server stops
+ * admitting. */
+typedef struct tc_server_config {
+    double hbm_budget_frac;   /* budget = this x device memory (0: 0.8) */
+    int64_t hbm_budget_bytes; /* > 0: explicit budget in bytes */
+    int32_t max_batch;        /* graphs per batched launch (0: 256) */
+    int32_t tie;              /* orientation tie-break of admitted edge lists */
+    int32_t batch_timeout_ms; /* watchdog on one batched launch (0: 60000) */
+    int32_t reserved;
+} tc_server_config;
+
+typedef struct tc_server_stats {
+    int64_t submitted, completed, failed, batches, cache_hits, evictions, max_batch_seen;
+    int64_t budget_bytes, used_bytes, resident_graphs, queued;
+} tc_server_stats;
+
+TC_API int tc_server_create(tc_ctx *ctx, const tc_server_config *cfg, tc_server **out);
+/* Queue a count.  graph_key != 0 keeps the oriented graph resident under that
+ * key; a later request with the same key is counted without preprocessing (it
+ * may then pass no edges).  The edge arrays are copied before returning. */
+TC_API int tc_server_submit(tc_server *s, uint64_t graph_key, const int64_t *src, const int64_t *dst, int64_t n_edges,
+                            int64_t n_nodes, uint64_t *request_id);
+/* TC_OK with the count and the latency (submit -> result) once done; the
+ * request's own error status if it failed; TC_E_NOT_READY before.  A result
+ * is handed out once. */
+TC_API int tc_server_poll(tc_server *s, uint64_t request_id, uint64_t *count, double *latency_ms);
+/* As poll, blocking up to timeout_ms (< 0: no limit); TC_E_TIMEOUT after it. */
+TC_API int tc_server_wait(tc_server *s, uint64_t request_id, int64_t timeout_ms, uint64_t *count, double *latency_ms);
+TC_API int tc_server_get_stats(tc_server *s, tc_server_stats *out);
+/* Finishes admitted work, fails requests still queued, frees everything. */
+TC_API int tc_server_destroy(tc_server *s);
+
 /* ---- host utilities: text files (the reference's on-disk contract) -------- */
 /* Parse a whitespace-separated file of unsigned integers into a flat array,
  * in file order, as the reference's fscanf loops read it
@@ -263,6 +309,9 @@ TC_API int tc_gen_chung_lu(int64_t n, double gamma, double avg_deg, uint64_t see
 /* Seeded uniform part assignment in [0, k) (replaces the unseeded
  * np.random.randint, Halo_creation_preprocess.py:288, 325, 362). */
 TC_API int tc_gen_parts_random(int64_t n, int k, uint64_t seed, int32_t *part);
+/* Contiguous assignment exactly as Halo_creation_preprocess.py:293-299:
+ * l = n / k, vertices [i*l, (i+1)*l) -> part i, the last n mod k -> part 0. */
+TC_API int tc_gen_parts_contig(int64_t n, int k, int32_t *part);
 
 #ifdef __cplusplus
 }

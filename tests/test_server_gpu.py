@@ -1,0 +1,87 @@
+"""Serving loop: continuous batching over resident graphs.  Each result is
+the same alone and in the mix (exact integers), resident graphs are reused
+by key and evicted LRU under the budget, and the host-side watchdog turns an
+over-long batch into TC_E_TIMEOUT without any device-side fault."""
+import threading
+
+import numpy as np
+import pytest
+
+import oracle
+import trianglecount_gb300 as tc
+from trianglecount_gb300 import generators as gen
+
+pytestmark = pytest.mark.gpu
+
+
+def _graphs():
+    out = [gen.rmat(s, seed=100 + s) for s in (10, 12, 14, 15)]
+    out += [gen.chung_lu(20000, 10.0, seed=7), gen.er(5000, 20.0, seed=8), gen.road(80)]
+    return out
+
+
+def test_results_identical_alone_and_in_the_mix(ctx):
+    gs = _graphs()
+    alone = [ctx.count(ctx.graph_from_edges(s, d)) for s, d in gs]
+    assert alone[0] == oracle.pipeline(*gs[0])[2]
+    with tc.Server(ctx, max_batch=64) as srv:
+        ids = [srv.submit(s, d, key=0) for s, d in gs for _ in range(3)]
+        got = [srv.wait(i)[0] for i in ids]
+        st = srv.stats()
+    assert got == [a for a in alone for _ in range(3)]
+    assert st["completed"] == len(ids) and st["failed"] == 0 and st["batches"] >= 1
+
+
+def test_resident_reuse_and_lru_eviction(ctx):
+    gs = _graphs()[:4]
+    want = [ctx.count(ctx.graph_from_edges(s, d)) for s, d in gs]
+    # a budget that holds about two of the graphs at a time
+    with tc.Server(ctx, hbm_budget_bytes=48 << 20, max_batch=8) as srv:
+        for rnd in range(3):
+            for k, (s, d) in enumerate(gs):
+                c, lat = srv.wait(srv.submit(s, d, key=k + 1))
+                assert c == want[k] and lat > 0
+        rid = srv.submit(key=4)  # most recently used: still resident, no edges needed
+        assert srv.wait(rid)[0] == want[3]
+        st = srv.stats()
+    assert st["evictions"] > 0 and st["cache_hits"] >= 1 and st["used_bytes"] <= st["budget_bytes"]
+
+
+def test_request_errors_and_concurrent_clients(ctx):
+    s, d = gen.rmat(12)
+    want = ctx.count(ctx.graph_from_edges(s, d))
+    with tc.Server(ctx, hbm_budget_bytes=8 << 20) as srv:
+        big = srv.submit(*gen.rmat(18), key=0)  # needs more than the whole budget
+        with pytest.raises(tc.TCError) as e:
+            srv.wait(big)
+        assert e.value.code == "TC_E_NOMEM"
+        with pytest.raises(tc.TCError) as e:
+            srv.wait(srv.submit(key=12345))  # unknown key and no edges
+        assert e.value.code == "TC_E_STATE"
+        results, errs = [], []
+
+        def client():
+            try:
+                for _ in range(5):
+                    results.append(srv.wait(srv.submit(s, d))[0])
+            except Exception as ex:  # reported below
+                errs.append(ex)
+
+        th = [threading.Thread(target=client) for _ in range(4)]
+        [t.start() for t in th]
+        [t.join() for t in th]
+        assert not errs and results == [want] * 20
+
+
+def test_batch_watchdog_reports_timeout(ctx):
+    """A 1 ms limit on a batch that takes longer: the request fails with
+    TC_E_TIMEOUT (the launch itself completes normally on the device) and the
+    server stops admitting new work."""
+    s, d = gen.rmat(18)
+    with tc.Server(ctx, batch_timeout_ms=1) as srv:
+        with pytest.raises(tc.TCError) as e:
+            srv.wait(srv.submit(s, d))
+        assert e.value.code == "TC_E_TIMEOUT"
+        with pytest.raises(tc.TCError) as e:
+            srv.wait(srv.submit(*gen.rmat(8)))
+        assert e.value.code == "TC_E_STATE"

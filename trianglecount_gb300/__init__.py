@@ -6,6 +6,6 @@ package is its Python host side: ctypes bindings, the reference's file
 formats and seeded synthetic inputs.
 """
 from ._native import TCError, lib  # noqa: F401
-from .api import Batch, Context, Graph, UGraph  # noqa: F401
+from .api import Batch, Context, Graph, Server, UGraph  # noqa: F401
 
-__all__ = ["Context", "Graph", "UGraph", "Batch", "TCError", "lib"]
+__all__ = ["Context", "Graph", "UGraph", "Batch", "Server", "TCError", "lib"]

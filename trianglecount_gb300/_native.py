@@ -38,6 +38,17 @@ class CountStats(C.Structure):
                 ("launches", C.c_int32), ("heavy_units", C.c_int32)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_frac", C.c_double), ("hbm_budget_bytes", C.c_int64), ("max_batch", C.c_int32),
+                ("tie", C.c_int32), ("batch_timeout_ms", C.c_int32), ("reserved", C.c_int32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "failed", "batches", "cache_hits", "evictions",
+                                         "max_batch_seen", "budget_bytes", "used_bytes", "resident_graphs",
+                                         "queued")]
+
+
 vp = C.c_void_p
 i64 = C.c_int64
 i32 = C.c_int32
@@ -57,6 +68,7 @@ _SIGS = {
     "tc_ctx_device_info": (C.c_int, [vp, P(C.c_int), P(C.c_size_t), P(C.c_size_t)]),
     "tc_ctx_get_tuning": (C.c_int, [vp, P(Tuning)]),
     "tc_ctx_set_tuning": (C.c_int, [vp, P(Tuning)]),
+    "tc_autotune": (C.c_int, [vp, vp, C.c_int, C.c_int, P(Tuning), P(C.c_float)]),
     "tc_graph_upload_i32": (C.c_int, [vp, vp, vp, i64, i64, i64, P(vp)]),
     "tc_graph_upload_u64": (C.c_int, [vp, vp, vp, i64, i64, i64, P(vp)]),
     "tc_graph_wrap_device_i32": (C.c_int, [vp, vp, vp, i64, i64, i64, P(vp)]),
@@ -82,6 +94,12 @@ _SIGS = {
     "tc_orient": (C.c_int, [vp, vp, C.c_int, P(vp)]),
     "tc_graph_from_edges": (C.c_int, [vp, vp, vp, i64, i64, C.c_int, P(vp)]),
     "tc_halo_extract": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, P(vp)]),
+    "tc_server_create": (C.c_int, [vp, P(ServerConfig), P(vp)]),
+    "tc_server_submit": (C.c_int, [vp, u64, vp, vp, i64, i64, P(u64)]),
+    "tc_server_poll": (C.c_int, [vp, u64, P(u64), P(C.c_double)]),
+    "tc_server_wait": (C.c_int, [vp, u64, i64, P(u64), P(C.c_double)]),
+    "tc_server_get_stats": (C.c_int, [vp, P(ServerStats)]),
+    "tc_server_destroy": (C.c_int, [vp]),
     "tc_text_read_u64": (C.c_int, [C.c_char_p, P(P(u64)), P(i64)]),
     "tc_host_free": (None, [vp]),
     "tc_text_write_line": (C.c_int, [C.c_char_p, vp, i64, C.c_int, C.c_char, C.c_int]),
@@ -96,6 +114,7 @@ _SIGS = {
     "tc_gen_er": (C.c_int, [i64, C.c_double, u64, vp, vp, P(i64)]),
     "tc_gen_chung_lu": (C.c_int, [i64, C.c_double, C.c_double, u64, vp, vp, i64]),
     "tc_gen_parts_random": (C.c_int, [i64, C.c_int, u64, vp]),
+    "tc_gen_parts_contig": (C.c_int, [i64, C.c_int, vp]),
 }
 
 _lib = None

@@ -155,6 +155,64 @@ class Batch:
             pass
 
 
+class Server:
+    """Continuous-batching triangle-count server (tc_server_* in the C ABI)."""
+
+    def __init__(self, ctx: "Context", hbm_budget_frac: float = 0.8, hbm_budget_bytes: int = 0,
+                 max_batch: int = 256, tie="reference", batch_timeout_ms: int = 60000):
+        cfg = N.ServerConfig(hbm_budget_frac, hbm_budget_bytes, max_batch, _tie(tie), batch_timeout_ms, 0)
+        h = C.c_void_p()
+        N.call("tc_server_create", ctx.handle, C.byref(cfg), C.byref(h))
+        self._h = h
+        self.ctx = ctx
+
+    def submit(self, src=None, dst=None, key: int = 0, n_nodes: int = 0) -> int:
+        rid = C.c_uint64()
+        if src is None:
+            N.call("tc_server_submit", self._h, int(key), None, None, 0, int(n_nodes), C.byref(rid))
+        else:
+            s = np.ascontiguousarray(src, np.int64)
+            d = np.ascontiguousarray(dst, np.int64)
+            N.call("tc_server_submit", self._h, int(key), _ptr(s), _ptr(d), len(s), int(n_nodes), C.byref(rid))
+        return rid.value
+
+    def poll(self, rid: int):
+        """(count, latency_ms) when done, None while pending; raises on failure."""
+        c, lat = C.c_uint64(), C.c_double()
+        st = N.lib().tc_server_poll(self._h, int(rid), C.byref(c), C.byref(lat))
+        if st == -7:
+            return None
+        N.check(st, "tc_server_poll")
+        return c.value, lat.value
+
+    def wait(self, rid: int, timeout_ms: int = -1):
+        c, lat = C.c_uint64(), C.c_double()
+        N.call("tc_server_wait", self._h, int(rid), int(timeout_ms), C.byref(c), C.byref(lat))
+        return c.value, lat.value
+
+    def stats(self) -> dict:
+        st = N.ServerStats()
+        N.call("tc_server_get_stats", self._h, C.byref(st))
+        return {k: getattr(st, k) for k, _ in N.ServerStats._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            N.lib().tc_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Context:
     """A CUDA device, a stream and libtc's scratch pool."""
 
@@ -211,6 +269,13 @@ class Context:
         t = N.Tuning(warp_max_deg, light_max_work, unit_work, long_list, blocks_per_sm)
         N.call("tc_ctx_set_tuning", self._h, C.byref(t))
 
+    def autotune(self, g: "Graph", max_trials: int = 32, reps: int = 3) -> tuple[dict, float]:
+        """Picks the fastest strategy thresholds for g by timing (sets them)."""
+        t = N.Tuning()
+        ms = C.c_float()
+        N.call("tc_autotune", self._h, g.handle, int(max_trials), int(reps), C.byref(t), C.byref(ms))
+        return {k: getattr(t, k) for k, _ in N.Tuning._fields_}, ms.value
+
     # ---- graphs ----
     def upload(self, row_ptr: np.ndarray, col: np.ndarray, n_roots: int | None = None) -> Graph:
         """Upload an oriented CSR (int32, or u64 narrowed on the device)."""
@@ -258,6 +323,9 @@ class Context:
 
     def batch(self, graphs: Sequence[Graph]) -> Batch:
         return Batch(self, graphs)
+
+    def server(self, **kw) -> "Server":
+        return Server(self, **kw)
 
     # ---- preprocessing ----
     def ugraph_from_edges(self, src: np.ndarray, dst: np.ndarray, n_nodes: int = 0) -> UGraph:

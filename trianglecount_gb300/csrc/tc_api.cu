@@ -1,8 +1,10 @@
 // tc_api.cu -- C ABI: contexts, oriented graphs, plain and batched counting.
 #include <algorithm>
+#include <chrono>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "tc_internal.h"
@@ -224,6 +226,95 @@ void scratch_free(CountScratch *sc, cudaStream_t s) {
     dfree(sc->out_work, s);
     dfree(sc->in_list, s);
     *sc = CountScratch();
+}
+
+int graph_rebind(tc_graph *g, tc_ctx *ctx) {
+    if (!g || !ctx) return set_error(TC_E_INVALID, "null argument");
+    if (g->ctx == ctx) return TC_OK;
+    if (g->ctx->device != ctx->device) return set_error(TC_E_INVALID, "graphs move only between contexts of one device");
+    TC_CUDA(cudaStreamSynchronize(g->ctx->stream));
+    ctx_retain(ctx);
+    tc_ctx *old = g->ctx;
+    g->ctx = ctx;
+    g->desc_valid = false;
+    ctx_release(old);
+    return TC_OK;
+}
+
+size_t graph_device_bytes(const tc_graph *g) {
+    const size_t csr = sizeof(int32_t) * (size_t)(g->n_rows + 1 + g->nnz);
+    const size_t scratch = (size_t)(g->n_rows + 1) * (4 + 4 + 8 + 8 + 16) + (size_t)g->nnz * 4 + 1024;
+    return csr + scratch;
+}
+
+int count_graphs_direct(tc_ctx *ctx, tc_graph *const *graphs, int n, uint64_t *outs, int64_t timeout_ms,
+                        float *kernel_ms) {
+    if (!ctx || n <= 0 || !graphs || !outs) return set_error(TC_E_INVALID, "bad batch arguments");
+    cudaStream_t s = ctx->stream;
+    std::vector<GraphDesc> desc((size_t)n);
+    int64_t chunks = 0, cap = 0, vtot = 0, etot = 0;
+    for (int i = 0; i < n; ++i) {
+        const tc_graph *g = graphs[i];
+        if (!g || g->ctx->device != ctx->device) return set_error(TC_E_INVALID, "graph %d is null or on another device", i);
+        memset(&desc[(size_t)i], 0, sizeof(GraphDesc));
+        desc[(size_t)i].rp = g->rp;
+        desc[(size_t)i].col = g->col;
+        desc[(size_t)i].n_rows = g->n_rows;
+        desc[(size_t)i].n_roots = g->n_roots;
+        desc[(size_t)i].chunk_base = chunks;
+        desc[(size_t)i].vbase = vtot;
+        chunks += (g->n_rows + 31) / 32;
+        vtot += g->n_rows + 1;
+        etot += g->nnz;
+        cap += std::min(g->n_rows, g->nnz) + 1;
+    }
+    CountScratch sc;
+    DBuf<GraphDesc> d_desc;
+    DBuf<unsigned char> d_work;
+    int st = d_desc.alloc((size_t)n, s);
+    if (st == TC_OK) st = d_work.alloc(sizeof(CountWork) + sizeof(unsigned long long) * (size_t)n, s);
+    if (st == TC_OK) st = scratch_alloc(&sc, vtot, chunks, etot, cap, s);
+    std::vector<unsigned char> h_out(sizeof(CountWork) + sizeof(unsigned long long) * (size_t)n);
+    if (st == TC_OK && cudaMemcpyAsync(d_desc.p, desc.data(), sizeof(GraphDesc) * (size_t)n, cudaMemcpyHostToDevice,
+                                       s) != cudaSuccess)
+        st = set_error(TC_E_CUDA, "descriptor upload failed");
+    if (st == TC_OK && cudaEventRecord(ctx->ev[0], s) != cudaSuccess) st = set_error(TC_E_CUDA, "event record failed");
+    if (st == TC_OK)
+        st = launch_count(d_desc.p, n, chunks, vtot, sc, (CountWork *)d_work.p,
+                          (unsigned long long *)(d_work.p + sizeof(CountWork)), false, ctx->tuned, s, nullptr);
+    if (st == TC_OK && cudaEventRecord(ctx->ev[1], s) != cudaSuccess) st = set_error(TC_E_CUDA, "event record failed");
+    if (st == TC_OK && cudaMemcpyAsync(h_out.data(), d_work.p, h_out.size(), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        st = set_error(TC_E_CUDA, "result read-back failed");
+    if (st == TC_OK && cudaEventRecord(ctx->ev[2], s) != cudaSuccess) st = set_error(TC_E_CUDA, "event record failed");
+    if (st == TC_OK) {
+        // bounded host wait on the launch: poll the event, give up after timeout_ms
+        const auto t0 = std::chrono::steady_clock::now();
+        for (;;) {
+            const cudaError_t q = cudaEventQuery(ctx->ev[2]);
+            if (q == cudaSuccess) break;
+            if (q != cudaErrorNotReady) {
+                st = cuda_error(q, "batched count", __FILE__, __LINE__);
+                break;
+            }
+            if (timeout_ms > 0 && std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(timeout_ms)) {
+                // the buffers must outlive the launch still in flight: leak them
+                d_desc.release();
+                d_work.release();
+                sc = CountScratch();
+                return set_error(TC_E_TIMEOUT, "batched count of %d graphs did not finish in %lld ms", n,
+                                 (long long)timeout_ms);
+            }
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+        }
+    }
+    if (st == TC_OK) {
+        const CountWork *w = (const CountWork *)h_out.data();
+        if (w->error) st = set_error(TC_E_STATE, "heavy-unit list overflow");
+        else memcpy(outs, h_out.data() + sizeof(CountWork), sizeof(uint64_t) * (size_t)n);
+        if (kernel_ms) cudaEventElapsedTime(kernel_ms, ctx->ev[0], ctx->ev[1]);
+    }
+    scratch_free(&sc, s);
+    return st;
 }
 
 int device_sm_count(int device) {

@@ -449,6 +449,15 @@ int tc_gen_chung_lu(int64_t n, double gamma, double avg_deg, uint64_t seed, int6
     return TC_OK;
 }
 
+int tc_gen_parts_contig(int64_t n, int k, int32_t *part) {
+    // Halo_creation_preprocess.py:293-299: l = N // k; parts[i*l:(i+1)*l] = i on
+    // a zero-filled array, so the last N mod k vertices stay in part 0.
+    if (n < 0 || k < 1 || (n > 0 && !part)) return set_error(TC_E_INVALID, "bad partition arguments");
+    const int64_t l = n / k;
+    for (int64_t v = 0; v < n; ++v) part[v] = (l > 0 && v < l * k) ? (int32_t)(v / l) : 0;
+    return TC_OK;
+}
+
 int tc_gen_parts_random(int64_t n, int k, uint64_t seed, int32_t *part) {
     if (n < 0 || k < 1 || (n > 0 && !part)) return set_error(TC_E_INVALID, "bad partition arguments");
     for (int64_t v = 0; v < n; ++v) part[v] = (int32_t)bounded(rng_at(seed, 5, (uint64_t)v), (uint64_t)k);

@@ -146,6 +146,16 @@ int radix_sort_u64(uint64_t **keys, uint64_t **tmp, int64_t n, int bits, cudaStr
 
 int device_sm_count(int device);
 
+// Counts n graphs (same device) with one batched launch on ctx's stream and
+// waits up to timeout_ms for the results (TC_E_TIMEOUT after that; the
+// launch is then still in flight).  Scratch comes from the stream-ordered pool.
+int count_graphs_direct(tc_ctx *ctx, tc_graph *const *graphs, int n, uint64_t *outs, int64_t timeout_ms,
+                        float *kernel_ms);
+// Moves a graph to another context of the same device (reference counts follow).
+int graph_rebind(tc_graph *g, tc_ctx *ctx);
+// Device bytes held by a graph (CSR + count scratch once sized).
+size_t graph_device_bytes(const tc_graph *g);
+
 // Context lifetime: every graph, ugraph and batch holds a reference to its
 // context, so tc_ctx_destroy only drops the caller's reference and the
 // context is freed when its last object is destroyed.

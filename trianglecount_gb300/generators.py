@@ -84,6 +84,13 @@ def parts_random(n: int, k: int, seed: int | None = None) -> np.ndarray:
     return part
 
 
+def parts_contig(n: int, k: int) -> np.ndarray:
+    """Contiguous parts as Halo_creation_preprocess.py:293-299 builds them."""
+    part = np.empty(n, np.int32)
+    N.call("tc_gen_parts_contig", n, k, _p(part))
+    return part
+
+
 class SplitMix64:
     """Deterministic parameter draws (same on every platform)."""
 
