@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--requests", type=int, default=150, help="serve: requests per rate")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-ref-kernel", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default thresholds (no autotuning)")
     return ap.parse_args()
 
 
@@ -225,6 +226,12 @@ def run_ours(args, world, rank, local, pg):
     t0 = time.perf_counter()
     g = ctx.graph_from_edges(src, dst)
     prep_s = time.perf_counter() - t0
+    tuning, tune_ms = ({}, None)
+    if not args.no_tune:  # per-graph strategy thresholds, picked on the device before timing
+        t0 = time.perf_counter()
+        tuning, tune_ms = ctx.autotune(g, max_trials=40)
+        cfg["autotune_s"] = round(time.perf_counter() - t0, 3)
+    cfg["tuning"] = tuning or ctx.get_tuning()
     rp, col = g.download()
     V, E = len(rp) - 1, len(col)
     dplus = np.diff(rp).astype(np.int64)

@@ -82,20 +82,23 @@ TC_API int tc_ctx_synchronize(tc_ctx *ctx);
 TC_API int tc_ctx_device_info(tc_ctx *ctx, int *sm_count, size_t *free_bytes, size_t *total_bytes);
 
 /* Strategy thresholds of the counting kernel (picked by the autotuner).
- * The classifier computes, per root u, d+(u) and its work
- * w(u) = sum_{v in N+(u)} d+(v) (one probe per oriented wedge).  Light roots
- * (d+(u) <= warp_max_deg and w(u) <= light_max_work) are counted by one warp
- * with a per-warp shared-memory hash of N+(u); heavy roots are split into
- * block units of about unit_work probes, each probing a shared hash of one
- * tile of N+(u).  Per out-neighbour v, lists with d+(v) >= long_list are
- * streamed by the whole warp; shorter lists are flattened across the lanes.
- * In tc_ctx_set_tuning, fields <= 0 (long_list, blocks_per_sm: < 0) keep
- * the current value. */
+ * The classifier computes, per vertex task x, d+(x) and its work (the probes
+ * of its partners' lists).  Light tasks (d+(x) <= warp_max_deg and work <=
+ * light_max_work) run on one warp with a per-warp shared-memory hash of
+ * N+(x); heavy ones are split into block units of about unit_work probes over
+ * a shared hash of one tile of N+(x).  Per partner, lists with length >=
+ * long_list are streamed by the whole warp; shorter lists are flattened
+ * across the lanes.  probe_kicks > 0 selects a cuckoo hash (two fixed probe
+ * slots per lookup, at most probe_kicks displacements per insertion, falling
+ * back to linear probing for a task whose insertion gives up); 0 selects
+ * linear probing.  In tc_ctx_set_tuning, fields <= 0 (long_list, probe_kicks,
+ * blocks_per_sm: < 0) keep the current value. */
 typedef struct tc_tuning {
     int32_t warp_max_deg;   /* 32..512, power of two */
-    int32_t light_max_work; /* wedge probes a light root may have */
+    int32_t light_max_work; /* wedge probes a light task may have */
     int32_t unit_work;      /* target wedge probes per heavy block unit */
     int32_t long_list;      /* 0..4096 */
+    int32_t probe_kicks;    /* 0..1024 */
     int32_t blocks_per_sm;  /* persistent grid = SMs * this (0: occupancy) */
 } tc_tuning;
 TC_API int tc_ctx_get_tuning(tc_ctx *ctx, tc_tuning *out);

@@ -13,10 +13,12 @@ from trianglecount_gb300 import generators as gen
 pytestmark = pytest.mark.gpu
 
 TUNINGS = [
-    {},  # defaults
+    {},  # defaults (cuckoo hash)
     {"warp_max_deg": 32, "light_max_work": 1, "unit_work": 1, "long_list": 0},  # heavy path everywhere, 32-v slices
-    {"warp_max_deg": 512, "light_max_work": 1 << 30, "unit_work": 1 << 30, "long_list": 4096},  # warps only, flattened
+    {"warp_max_deg": 512, "light_max_work": 1 << 30, "unit_work": 1 << 30, "long_list": 4096,
+     "probe_kicks": 0},  # warps only, flattened, linear probing
     {"warp_max_deg": 64, "light_max_work": 500, "unit_work": 3000, "long_list": 5, "blocks_per_sm": 1},
+    {"probe_kicks": 1},  # cuckoo insertions give up often: exercises the linear-probing fallback
 ]
 
 
@@ -24,7 +26,8 @@ TUNINGS = [
 def tuned(ctx):
     old = ctx.get_tuning()
     yield ctx
-    ctx.set_tuning(old["warp_max_deg"], old["light_max_work"], old["unit_work"], old["long_list"], 0)
+    ctx.set_tuning(old["warp_max_deg"], old["light_max_work"], old["unit_work"], old["long_list"],
+                   old["probe_kicks"], 0)
 
 
 @pytest.mark.parametrize("tuning", TUNINGS)

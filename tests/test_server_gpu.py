@@ -35,8 +35,10 @@ def test_results_identical_alone_and_in_the_mix(ctx):
 def test_resident_reuse_and_lru_eviction(ctx):
     gs = _graphs()[:4]
     want = [ctx.count(ctx.graph_from_edges(s, d)) for s, d in gs]
-    # a budget that holds about two of the graphs at a time
-    with tc.Server(ctx, hbm_budget_bytes=48 << 20, max_batch=8) as srv:
+    # a budget just above the build footprint of the largest graph (about 58
+    # bytes per input edge), so residents must be evicted to build it again
+    budget = 58 * max(len(s) for s, _ in gs) + (3 << 20)
+    with tc.Server(ctx, hbm_budget_bytes=budget, max_batch=8) as srv:
         for rnd in range(3):
             for k, (s, d) in enumerate(gs):
                 c, lat = srv.wait(srv.submit(s, d, key=k + 1))

@@ -389,10 +389,11 @@ int tc_ctx_create(int device, tc_ctx **out) {
     tc_ctx *c = new tc_ctx();
     c->device = device;
     c->sm_count = device_sm_count(device);
-    c->tuning.warp_max_deg = 128;
-    c->tuning.light_max_work = 32768;
+    c->tuning.warp_max_deg = 256;
+    c->tuning.light_max_work = 8192;
     c->tuning.unit_work = 262144;
-    c->tuning.long_list = 16;
+    c->tuning.long_list = 32;
+    c->tuning.probe_kicks = 32;
     c->tuning.blocks_per_sm = 0;
     int st = TC_OK;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) st = TC_E_CUDA;
@@ -457,6 +458,7 @@ int tc_ctx_set_tuning(tc_ctx *c, const tc_tuning *in) {
     if (in->light_max_work > 0) t.light_max_work = in->light_max_work;
     if (in->unit_work > 0) t.unit_work = in->unit_work;
     if (in->long_list >= 0) t.long_list = in->long_list;
+    if (in->probe_kicks >= 0) t.probe_kicks = in->probe_kicks;
     if (in->blocks_per_sm >= 0) t.blocks_per_sm = in->blocks_per_sm;
     Tuned r;
     TC_TRY(resolve_tuning(t, c->sm_count, &r));

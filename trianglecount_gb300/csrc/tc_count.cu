@@ -63,6 +63,12 @@ constexpr int kEmpty = -1;
 constexpr int kThreads = 256;
 constexpr int kWarpsPerBlock = kThreads / kWarp;
 constexpr int kHeavyChunk = 4;  // partners per warp grab inside a heavy unit
+#ifndef TC_COUNT_MIN_BLOCKS
+// Resident blocks per SM the count kernel's registers must allow: 6 caps it
+// at 40 registers (a few spilled bytes) for 48 warps per SM, ~10% faster on
+// R-MAT than the unconstrained 48 registers / 40 warps.
+#define TC_COUNT_MIN_BLOCKS 6
+#endif
 
 __device__ __forceinline__ uint32_t hash_slot(int x, int shift) { return ((uint32_t)x * 0x9E3779B1u) >> shift; }
 
@@ -88,6 +94,40 @@ __device__ __forceinline__ uint32_t table_probe(const int *tab, uint32_t mask, i
         y = tab[h];
     }
     return (uint32_t)(y == x);
+}
+
+// Cuckoo hashing (two slots per key, Pagh & Rodler; parallel insertion by
+// atomicExch as in Alcantara et al., "Real-time parallel hashing on the GPU",
+// 2009): a lookup reads exactly the two candidate slots -- two independent
+// shared loads, no loop, so the lanes of a warp never diverge on collisions.
+// Insertion moves a displaced key to its other slot, at most `kicks` times;
+// every key is always either in the table or in one thread's hand, so when no
+// insertion gives up, all keys are in.  A give-up switches the task to linear
+// probing (rebuilt), decided warp- or block-uniformly.
+__device__ __forceinline__ uint32_t hash_slot2(int x, int shift) { return ((uint32_t)x * 0x85EBCA77u) >> shift; }
+
+__device__ __forceinline__ bool cuckoo_insert(int *tab, int shift, int x, int kicks) {
+    int cur = x;
+    uint32_t pos = hash_slot(cur, shift);
+    for (int it = 0; it < kicks; ++it) {
+        const int old = atomicExch(&tab[pos], cur);
+        if (old == kEmpty) return true;
+        cur = old;
+        const uint32_t p1 = hash_slot(cur, shift), p2 = hash_slot2(cur, shift);
+        pos = pos == p1 ? p2 : p1;
+    }
+    return false;
+}
+
+__device__ __forceinline__ uint32_t cuckoo_probe(const int *tab, int shift, int x) {
+    const int a = tab[hash_slot(x, shift)];
+    const int b = tab[hash_slot2(x, shift)];
+    return (uint32_t)((a == x) | (b == x));
+}
+
+// Membership of x >= 0 in the table, by the table's mode.
+__device__ __forceinline__ uint32_t probe_any(const int *tab, uint32_t mask, int shift, int x, bool cuckoo) {
+    return cuckoo ? cuckoo_probe(tab, shift, x) : table_probe(tab, mask, shift, x);
 }
 
 // Table geometry for n keys: slots = max(32, next_pow2(4 n)).
@@ -135,6 +175,7 @@ struct KParams {
     int unit_work;
     int tile;
     int long_list;
+    int probe_kicks;  // 0: linear probing; > 0: cuckoo with this many kicks
 };
 
 // Where the partner p_j of task x lives and whose root it credits.
@@ -154,7 +195,7 @@ struct Task {
 template <bool kPerRoot>
 __device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
                                                    const Task &T, int j0, int j1, const int *tab, uint32_t mask,
-                                                   int shift, int long_list, int lane,
+                                                   int shift, bool cuckoo, int long_list, int lane,
                                                    unsigned long long *__restrict__ per_root) {
     uint32_t hits = 0;
     const int j = j0 + lane;
@@ -187,9 +228,14 @@ __device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ r
                 const int t = base + i * kWarp + lane;
                 x[i] = t < ll ? __ldg(p + t) : -1;
             }
+            if (cuckoo) {
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
-                if (x[i] >= 0) h += table_probe(tab, mask, shift, x[i]);
+                for (int i = 0; i < 4; ++i) h += (uint32_t)(x[i] >= 0) & cuckoo_probe(tab, shift, x[i]);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    if (x[i] >= 0) h += table_probe(tab, mask, shift, x[i]);
+            }
         }
         hits += h;
         if (kPerRoot) {
@@ -221,7 +267,7 @@ __device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ r
         const int s_seg = __shfl_sync(kFull, s2, seg);
         const int own = kPerRoot ? __shfl_sync(kFull, owner, seg) : 0;
         if (t < total) {
-            const uint32_t h = table_probe(tab, mask, shift, __ldg(col + s_seg + (t - ex_seg)));
+            const uint32_t h = probe_any(tab, mask, shift, __ldg(col + s_seg + (t - ex_seg)), cuckoo);
             hits += h;
             if (kPerRoot && h) atomicAdd(per_root + own, 1ull);
         }
@@ -343,7 +389,7 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
 }
 
 template <bool kPerRoot>
-__global__ void __launch_bounds__(kThreads) count_kernel(KParams P) {
+__global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KParams P) {
     extern __shared__ int smem[];
     __shared__ unsigned s_unit;
     __shared__ int s_entry;
@@ -367,6 +413,7 @@ __global__ void __launch_bounds__(kThreads) count_kernel(KParams P) {
 
     // ---- phase A: heavy units, one block each ----
     int cached_entry = -1, cached_tile = -1;
+    bool cached_cuckoo = false;
     for (;;) {
         if (warp == 0) {
             unsigned unit = 0;
@@ -422,7 +469,19 @@ __global__ void __launch_bounds__(kThreads) count_kernel(KParams P) {
         if (ei != cached_entry || ti != cached_tile) {
             table_clear(smem, mask, threadIdx.x, kThreads);
             __syncthreads();
-            for (int i = threadIdx.x; i < tl; i += kThreads) table_insert(smem, mask, shift, __ldg(col + rs + t0 + i));
+            bool ok = true;
+            if (P.probe_kicks > 0)
+                for (int i = threadIdx.x; i < tl; i += kThreads)
+                    ok &= cuckoo_insert(smem, shift, __ldg(col + rs + t0 + i), P.probe_kicks);
+            cached_cuckoo = P.probe_kicks > 0 && !__syncthreads_or(!ok);
+            if (!cached_cuckoo) {  // linear probing (chosen, or after a cuckoo give-up)
+                if (P.probe_kicks > 0) {
+                    table_clear(smem, mask, threadIdx.x, kThreads);
+                    __syncthreads();
+                }
+                for (int i = threadIdx.x; i < tl; i += kThreads)
+                    table_insert(smem, mask, shift, __ldg(col + rs + t0 + i));
+            }
             cached_entry = ei;
             cached_tile = ti;
         }
@@ -436,8 +495,8 @@ __global__ void __launch_bounds__(kThreads) count_kernel(KParams P) {
             c = __shfl_sync(kFull, c, 0);
             const int jb = j0 + c * kHeavyChunk;
             if (jb >= j1) break;
-            hits += probe_partners<kPerRoot>(rp, col, T, jb, min(jb + kHeavyChunk, j1), smem, mask, shift, P.long_list,
-                                             lane, G.per_root);
+            hits += probe_partners<kPerRoot>(rp, col, T, jb, min(jb + kHeavyChunk, j1), smem, mask, shift,
+                                             cached_cuckoo, P.long_list, lane, G.per_root);
         }
         if (!kPerRoot) {
             if (e.g != cur_g) flush(e.g);
@@ -485,11 +544,22 @@ __global__ void __launch_bounds__(kThreads) count_kernel(KParams P) {
             const int shift = 32 - lg;
             table_clear(wtab, mask, lane, kWarp);
             __syncwarp();
-            for (int i = lane; i < T.dx; i += kWarp) table_insert(wtab, mask, shift, __ldg(col + rrs + i));
+            bool ok = true;
+            if (P.probe_kicks > 0)
+                for (int i = lane; i < T.dx; i += kWarp) ok &= cuckoo_insert(wtab, shift, __ldg(col + rrs + i), P.probe_kicks);
+            const bool cuckoo = P.probe_kicks > 0 && __all_sync(kFull, ok);
+            if (!cuckoo) {  // linear probing (chosen, or after a cuckoo give-up)
+                if (P.probe_kicks > 0) {
+                    __syncwarp();
+                    table_clear(wtab, mask, lane, kWarp);
+                    __syncwarp();
+                }
+                for (int i = lane; i < T.dx; i += kWarp) table_insert(wtab, mask, shift, __ldg(col + rrs + i));
+            }
             __syncwarp();
             uint32_t hits = 0;
             for (int jb = 0; jb < n_part; jb += kWarp)
-                hits += probe_partners<kPerRoot>(rp, col, T, jb, min(jb + kWarp, n_part), wtab, mask, shift,
+                hits += probe_partners<kPerRoot>(rp, col, T, jb, min(jb + kWarp, n_part), wtab, mask, shift, cuckoo,
                                                  P.long_list, lane, G.per_root);
             __syncwarp();
             if (!kPerRoot) acc += hits;
@@ -508,7 +578,7 @@ int pow2_floor_log(int x) {
 
 int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     Tuned r;
-    const int wm = t.warp_max_deg > 0 ? t.warp_max_deg : 128;
+    const int wm = t.warp_max_deg > 0 ? t.warp_max_deg : 256;
     if (wm < 32 || wm > 512 || (wm & (wm - 1)))
         return set_error(TC_E_INVALID, "warp_max_deg must be a power of two in [32, 512], got %d", wm);
     r.warp_max = wm;
@@ -517,9 +587,11 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     const int block_slots = std::max(8192, warp_slots_total);
     r.log_block_slots = pow2_floor_log(block_slots);
     r.tile = block_slots / 4;
-    r.light_max_work = t.light_max_work > 0 ? t.light_max_work : 32768;
+    r.light_max_work = t.light_max_work > 0 ? t.light_max_work : 8192;
     r.unit_work = t.unit_work > 0 ? t.unit_work : 262144;
-    r.long_list = t.long_list >= 0 ? t.long_list : 16;
+    r.long_list = t.long_list >= 0 ? t.long_list : 32;
+    r.probe_kicks = t.probe_kicks >= 0 ? t.probe_kicks : 32;
+    if (r.probe_kicks > 1024) return set_error(TC_E_INVALID, "probe_kicks must be <= 1024, got %d", r.probe_kicks);
     if (r.long_list > 4096) return set_error(TC_E_INVALID, "long_list must be <= 4096, got %d", r.long_list);
     r.threads = kThreads;
     r.smem = (size_t)block_slots * sizeof(int);
@@ -557,6 +629,7 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
     P.unit_work = tn.unit_work;
     P.tile = tn.tile;
     P.long_list = tn.long_list;
+    P.probe_kicks = tn.probe_kicks;
     TC_CUDA(cudaMemsetAsync(work, 0, sizeof(CountWork), s));
     TC_CUDA(cudaMemsetAsync(results, 0, sizeof(unsigned long long) * (size_t)n_graphs, s));
     int nl = 0;
@@ -603,6 +676,7 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
     P.unit_work = tn.unit_work;
     P.tile = tn.tile;
     P.long_list = tn.long_list;
+    P.probe_kicks = tn.probe_kicks;
     TC_CUDA(cudaMemsetAsync(work, 0, sizeof(CountWork), s));
     TC_CUDA(cudaMemsetAsync(results, 0, sizeof(unsigned long long), s));
     if (total_chunks > 0) {

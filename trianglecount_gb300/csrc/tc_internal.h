@@ -108,6 +108,7 @@ struct Tuned {  // resolved tc_tuning with derived table geometry
     int light_max_work;
     int unit_work;
     int long_list;
+    int probe_kicks;     // 0: linear-probing hash; > 0: cuckoo hash with this kick bound
     int tile;            // block table entries per tile (a quarter of its slots)
     int log_block_slots;
     int threads;         // per block

@@ -67,10 +67,11 @@ int setup_device(int dev, DeviceSetup **out) {
         void *p = nullptr;
         TC_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
         tc_tuning t{};
-        t.warp_max_deg = 128;
-        t.light_max_work = 32768;
+        t.warp_max_deg = 256;
+        t.light_max_work = 8192;
         t.unit_work = 262144;
-        t.long_list = 16;
+        t.long_list = 32;
+        t.probe_kicks = 32;
         t.blocks_per_sm = 0;
         TC_TRY(resolve_tuning(t, device_sm_count(dev), &d.tuned));
         d.scratch = (unsigned char *)p;

@@ -3,6 +3,7 @@
 // The thresholds decide, per vertex task, warp vs block execution
 // (warp_max_deg, light_max_work), the size of block units (unit_work) and,
 // per partner list, whole-warp streaming vs lane flattening (long_list).
+// probe_kicks picks the hash (cuckoo or linear probing).
 // Their best values depend on the degree distribution, so they are picked per
 // graph by timing the real count: coordinate descent from the current tuning,
 // one parameter at a time over a small candidate grid, repeated until a pass
@@ -42,20 +43,25 @@ extern "C" int tc_autotune(tc_ctx *ctx, tc_graph *g, int max_trials, int reps, t
     float cur_ms = 0;
     TC_TRY(time_count(ctx, g, reps, &cur_ms));
     int trials = 1;
-    const std::vector<int32_t> grid[4] = {
+    const std::vector<int32_t> grid[5] = {
         {64, 128, 256, 512},
         {4096, 8192, 16384, 32768, 65536, 131072},
         {65536, 131072, 262144, 524288, 1048576},
         {8, 16, 32, 64},
+        {0, 32},
     };
     bool changed = true;
     while (changed && trials < max_trials) {
         changed = false;
-        for (int p = 0; p < 4 && trials < max_trials; ++p) {
+        for (int p = 0; p < 5 && trials < max_trials; ++p) {
             for (int32_t v : grid[p]) {
                 if (trials >= max_trials) break;
                 tc_tuning t = cur;
-                int32_t *field = p == 0 ? &t.warp_max_deg : p == 1 ? &t.light_max_work : p == 2 ? &t.unit_work : &t.long_list;
+                int32_t *field = p == 0   ? &t.warp_max_deg
+                                 : p == 1 ? &t.light_max_work
+                                 : p == 2 ? &t.unit_work
+                                 : p == 3 ? &t.long_list
+                                          : &t.probe_kicks;
                 if (*field == v) continue;
                 *field = v;
                 TC_TRY(tc_ctx_set_tuning(ctx, &t));
