@@ -79,7 +79,7 @@ def test_batch_watchdog_reports_timeout(ctx):
     """A 1 ms limit on a batch that takes longer: the request fails with
     TC_E_TIMEOUT (the launch itself completes normally on the device) and the
     server stops admitting new work."""
-    s, d = gen.rmat(18)
+    s, d = gen.rmat(21)  # a count of several milliseconds
     with tc.Server(ctx, batch_timeout_ms=1) as srv:
         with pytest.raises(tc.TCError) as e:
             srv.wait(srv.submit(s, d))

@@ -209,6 +209,7 @@ int scratch_alloc(CountScratch *sc, int64_t V, int64_t C, int64_t E, int64_t hea
     sc->heavy_cap = heavy_cap;
     TC_TRY(dalloc((void **)&sc->heavy, sizeof(HeavyEntry) * (size_t)std::max<int64_t>(heavy_cap, 1), s));
     TC_TRY(dalloc((void **)&sc->light_mask, sizeof(uint32_t) * (size_t)std::max<int64_t>(C, 1), s));
+    TC_TRY(dalloc((void **)&sc->micro_mask, sizeof(uint32_t) * (size_t)std::max<int64_t>(C, 1), s));
     TC_TRY(dalloc((void **)&sc->in_cnt, sizeof(int32_t) * (size_t)std::max<int64_t>(V, 1), s));
     TC_TRY(dalloc((void **)&sc->in_off, sizeof(int32_t) * (size_t)(V + 1), s));
     TC_TRY(dalloc((void **)&sc->in_work, sizeof(unsigned long long) * (size_t)std::max<int64_t>(V, 1), s));
@@ -220,6 +221,7 @@ int scratch_alloc(CountScratch *sc, int64_t V, int64_t C, int64_t E, int64_t hea
 void scratch_free(CountScratch *sc, cudaStream_t s) {
     dfree(sc->heavy, s);
     dfree(sc->light_mask, s);
+    dfree(sc->micro_mask, s);
     dfree(sc->in_cnt, s);
     dfree(sc->in_off, s);
     dfree(sc->in_work, s);
@@ -243,7 +245,7 @@ int graph_rebind(tc_graph *g, tc_ctx *ctx) {
 
 size_t graph_device_bytes(const tc_graph *g) {
     const size_t csr = sizeof(int32_t) * (size_t)(g->n_rows + 1 + g->nnz);
-    const size_t scratch = (size_t)(g->n_rows + 1) * (4 + 4 + 8 + 8 + 16) + (size_t)g->nnz * 4 + 1024;
+    const size_t scratch = (size_t)(g->n_rows + 1) * (4 + 4 + 8 + 8 + 16 + 1) + (size_t)g->nnz * 4 + 1024;
     return csr + scratch;
 }
 

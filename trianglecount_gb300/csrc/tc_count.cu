@@ -63,6 +63,9 @@ constexpr int kEmpty = -1;
 constexpr int kThreads = 256;
 constexpr int kWarpsPerBlock = kThreads / kWarp;
 constexpr int kHeavyChunk = 4;  // partners per warp grab inside a heavy unit
+constexpr int kLaneRowDeg = 16; // auxiliary passes: rows with d+ <= this are walked one per lane
+constexpr int kMicroDeg = 8;    // micro tasks: d+(x) <= this (N+(x) held in registers) ...
+constexpr int kMicroWork = 512; // ... and at most this many probes (one lane runs the task)
 #ifndef TC_COUNT_MIN_BLOCKS
 // Resident blocks per SM the count kernel's registers must allow: 6 caps it
 // at 40 registers (a few spilled bytes) for 48 warps per SM, ~10% faster on
@@ -164,6 +167,7 @@ struct KParams {
     CountWork *work;
     unsigned long long *results;
     uint32_t *light_mask;  // one word per 32-row chunk
+    uint32_t *micro_mask;  // one word per 32-row chunk
     int32_t *in_cnt;       // per vertex (pooled): middle-centric in-edges, consumed by the transpose
     int32_t *in_off;       // per vertex (pooled) + 1: exclusive scan of in_cnt
     unsigned long long *in_work;   // per vertex: sum of d+(u) over its in-partners u
@@ -293,7 +297,23 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
             rs = __ldg(rp + x0 + lane);
             d = __ldg(rp + x0 + lane + 1) - rs;
         }
-        unsigned todo = __ballot_sync(kFull, d >= 1);
+        // short rows: one per lane
+        if (d >= 1 && d <= kLaneRowDeg) {
+            unsigned long long ow = 0;
+            for (int i = 0; i < d; ++i) {
+                const int v = __ldg(col + rs + i);
+                const int dv = __ldg(rp + v + 1) - __ldg(rp + v);
+                if (d < dv) {
+                    atomicAdd(P.in_cnt + G.vbase + v, 1);
+                    atomicAdd(P.in_work + G.vbase + v, (unsigned long long)d);
+                } else {
+                    ow += (unsigned long long)dv;
+                }
+            }
+            P.out_work[G.vbase + x0 + lane] = ow;
+        }
+        // long rows: the whole warp
+        unsigned todo = __ballot_sync(kFull, d > kLaneRowDeg);
         while (todo) {
             const int k = __ffs(todo) - 1;
             todo &= todo - 1u;
@@ -338,8 +358,19 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
             nin = P.in_off[G.vbase + x + 1] - P.in_off[G.vbase + x];
             w = P.out_work[G.vbase + x] + P.in_work[G.vbase + x];
         }
-        // scatter the middle-centric out-edges of the chunk's roots
-        unsigned todo = __ballot_sync(kFull, d >= 1 && x < G.n_roots);
+        // scatter the middle-centric out-edges of the chunk's roots: short rows one per lane ...
+        if (d >= 1 && d <= kLaneRowDeg && x < G.n_roots) {
+            for (int i = 0; i < d; ++i) {
+                const int v = __ldg(col + rs + i);
+                const int dv = __ldg(rp + v + 1) - __ldg(rp + v);
+                if (d < dv) {
+                    const int pos = atomicSub(P.in_cnt + G.vbase + v, 1) - 1;
+                    P.in_list[P.in_off[G.vbase + v] + pos] = (int32_t)x;
+                }
+            }
+        }
+        // ... long rows by the whole warp
+        unsigned todo = __ballot_sync(kFull, d > kLaneRowDeg && x < G.n_roots);
         while (todo) {
             const int k = __ffs(todo) - 1;
             todo &= todo - 1u;
@@ -356,10 +387,15 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
         }
         // classify
         const bool has = w > 0 && d >= 1;
-        const bool light = has && d <= P.warp_max && w <= (unsigned long long)P.light_max_work;
-        const bool hv = has && !light;
+        const bool micro = has && d <= kMicroDeg && w <= (unsigned long long)kMicroWork;
+        const bool light = has && !micro && d <= P.warp_max && w <= (unsigned long long)P.light_max_work;
+        const bool hv = has && !micro && !light;
+        const uint32_t mm = __ballot_sync(kFull, micro);
         const uint32_t lm = __ballot_sync(kFull, light);
-        if (lane == 0) P.light_mask[c] = lm;
+        if (lane == 0) {
+            P.light_mask[c] = lm;
+            P.micro_mask[c] = mm;
+        }
         unsigned hm = __ballot_sync(kFull, hv);
         while (hm) {
             const int k = __ffs(hm) - 1;
@@ -385,6 +421,82 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
                 }
             }
         }
+    }
+}
+
+// micro tasks: one lane runs a whole task x (d+(x) <= kMicroDeg, work <=
+// kMicroWork) with N+(x) in registers; every streamed partner list is then at
+// most kMicroDeg long (the cheaper side), and membership is kMicroDeg
+// predicated compares -- no hash table, no shared memory.
+template <bool kPerRoot>
+__global__ void __launch_bounds__(kThreads) micro_kernel(KParams P) {
+    const int lane = threadIdx.x & (kWarp - 1);
+    const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / kWarp;
+    unsigned long long acc = 0;
+    int cur_g = -1;
+    for (int64_t c = gwarp; c < P.total_chunks; c += nwarps) {
+        const uint32_t mm = P.micro_mask[c];
+        if (!mm) continue;
+        const int g = find_graph(P.gd, P.n_graphs, c);
+        const GraphDesc &G = P.gd[g];
+        if (!kPerRoot && g != cur_g) {
+            const unsigned long long s = warp_sum_u64(acc);
+            if (lane == 0 && cur_g >= 0 && s) atomicAdd(P.results + cur_g, s);
+            acc = 0;
+            cur_g = g;
+        }
+        if (!((mm >> lane) & 1u)) continue;
+        const int32_t *__restrict__ rp = G.rp;
+        const int32_t *__restrict__ col = G.col;
+        const int x = (int)((c - G.chunk_base) * kWarp + lane);
+        const int rs = __ldg(rp + x);
+        const int d = __ldg(rp + x + 1) - rs;
+        int r[kMicroDeg];
+#pragma unroll
+        for (int i = 0; i < kMicroDeg; ++i) r[i] = i < d ? __ldg(col + rs + i) : -1;
+        uint32_t own = 0;  // hits credited to x (root-centric partners)
+        if (x < G.n_roots) {
+#pragma unroll
+            for (int i = 0; i < kMicroDeg; ++i) {
+                if (i >= d) break;
+                const int p = r[i];
+                const int s2 = __ldg(rp + p);
+                const int len = __ldg(rp + p + 1) - s2;
+                if (len > d) continue;  // middle-centric: done from p's side
+                for (int t = 0; t < len; ++t) {
+                    const int y = __ldg(col + s2 + t);
+                    uint32_t hit = 0;
+#pragma unroll
+                    for (int q = 0; q < kMicroDeg; ++q) hit |= (uint32_t)(r[q] == y);
+                    own += hit;
+                }
+            }
+        }
+        uint32_t in_hits = 0;
+        const int i0 = P.in_off[G.vbase + x], i1 = P.in_off[G.vbase + x + 1];
+        for (int k = i0; k < i1; ++k) {
+            const int p = P.in_list[k];
+            const int s2 = __ldg(rp + p);
+            const int len = __ldg(rp + p + 1) - s2;
+            uint32_t hp = 0;
+            for (int t = 0; t < len; ++t) {
+                const int y = __ldg(col + s2 + t);
+#pragma unroll
+                for (int q = 0; q < kMicroDeg; ++q) hp += (uint32_t)(r[q] == y);
+            }
+            in_hits += hp;
+            if (kPerRoot && hp) atomicAdd(G.per_root + p, (unsigned long long)hp);
+        }
+        if (kPerRoot) {
+            if (own) atomicAdd(G.per_root + x, (unsigned long long)own);
+        } else {
+            acc += own + in_hits;
+        }
+    }
+    if (!kPerRoot) {
+        const unsigned long long s = warp_sum_u64(acc);
+        if (lane == 0 && cur_g >= 0 && s) atomicAdd(P.results + cur_g, s);
     }
 }
 
@@ -618,6 +730,7 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
     P.work = work;
     P.results = results;
     P.light_mask = sc.light_mask;
+    P.micro_mask = sc.micro_mask;
     P.in_cnt = sc.in_cnt;
     P.in_off = sc.in_off;
     P.in_work = sc.in_work;
@@ -644,10 +757,15 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
         TC_TRY(scan_exclusive_i32(sc.in_cnt, sc.in_off, total_vertices, s));
         transpose_classify_kernel<<<aux_blocks, kThreads, 0, s>>>(P, sc.heavy);
         TC_CUDA(cudaGetLastError());
-        if (per_root) count_kernel<true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
-        else count_kernel<false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        if (per_root) {
+            micro_kernel<true><<<aux_blocks, kThreads, 0, s>>>(P);
+            count_kernel<true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        } else {
+            micro_kernel<false><<<aux_blocks, kThreads, 0, s>>>(P);
+            count_kernel<false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        }
         TC_CUDA(cudaGetLastError());
-        nl = 3 + (total_vertices > 4096 ? 3 : 1);
+        nl = 4 + (total_vertices > 4096 ? 3 : 1);
     }
     if (launches) *launches = nl;
     return TC_OK;
@@ -665,6 +783,7 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
     P.work = work;
     P.results = results;
     P.light_mask = sc.light_mask;
+    P.micro_mask = sc.micro_mask;
     P.in_cnt = sc.in_cnt;
     P.in_off = sc.in_off;
     P.in_work = sc.in_work;
@@ -690,6 +809,7 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
         TC_TRY(scan_exclusive_i32_tmp(sc.in_cnt, sc.in_off, total_vertices, scan_tmp, scan_tmp_cap, s));
         transpose_classify_kernel<<<aux_blocks, kThreads, 0, s>>>(P, sc.heavy);
         TC_CUDA(cudaGetLastError());
+        micro_kernel<false><<<aux_blocks, kThreads, 0, s>>>(P);
         count_kernel<false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
         TC_CUDA(cudaGetLastError());
     }

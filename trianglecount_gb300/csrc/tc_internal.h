@@ -84,6 +84,7 @@ struct CountScratch {
     HeavyEntry *heavy = nullptr;  // heavy_cap entries
     int64_t heavy_cap = 0;
     uint32_t *light_mask = nullptr;         // C words
+    uint32_t *micro_mask = nullptr;         // C words
     int32_t *in_cnt = nullptr;              // V
     int32_t *in_off = nullptr;              // V + 1
     unsigned long long *in_work = nullptr;  // V
