@@ -58,8 +58,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["rmat21", "road", "rmat16", "rmat18", "rmat23", "rmat23_parts", "batch256",
                                            "serve"], default="rmat21")
-    ap.add_argument("--rates", default="20,80,320", help="serve: Poisson arrival rates (requests/s)")
-    ap.add_argument("--requests", type=int, default=150, help="serve: requests per rate")
+    ap.add_argument("--rates", default="50,200,1000,4000", help="serve: Poisson arrival rates (requests/s)")
+    ap.add_argument("--requests", type=int, default=400, help="serve: requests per rate")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-ref-kernel", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default thresholds (no autotuning)")

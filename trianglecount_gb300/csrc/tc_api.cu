@@ -273,10 +273,18 @@ int count_graphs_direct(tc_ctx *ctx, tc_graph *const *graphs, int n, uint64_t *o
     CountScratch sc;
     DBuf<GraphDesc> d_desc;
     DBuf<unsigned char> d_work;
+    const size_t out_bytes = sizeof(CountWork) + sizeof(unsigned long long) * (size_t)n;
+    // the read-back must go to page-locked memory: a copy into pageable memory
+    // blocks the host until the launch finishes, which would defeat the bounded wait
+    unsigned char *h_out = (unsigned char *)ctx->h_pinned;
+    unsigned char *h_own = nullptr;
+    if (out_bytes > 4096) {
+        if (cudaMallocHost(&h_own, out_bytes) != cudaSuccess) return set_error(TC_E_NOMEM, "pinned result buffer");
+        h_out = h_own;
+    }
     int st = d_desc.alloc((size_t)n, s);
-    if (st == TC_OK) st = d_work.alloc(sizeof(CountWork) + sizeof(unsigned long long) * (size_t)n, s);
+    if (st == TC_OK) st = d_work.alloc(out_bytes, s);
     if (st == TC_OK) st = scratch_alloc(&sc, vtot, chunks, etot, cap, s);
-    std::vector<unsigned char> h_out(sizeof(CountWork) + sizeof(unsigned long long) * (size_t)n);
     if (st == TC_OK && cudaMemcpyAsync(d_desc.p, desc.data(), sizeof(GraphDesc) * (size_t)n, cudaMemcpyHostToDevice,
                                        s) != cudaSuccess)
         st = set_error(TC_E_CUDA, "descriptor upload failed");
@@ -285,7 +293,7 @@ int count_graphs_direct(tc_ctx *ctx, tc_graph *const *graphs, int n, uint64_t *o
         st = launch_count(d_desc.p, n, chunks, vtot, sc, (CountWork *)d_work.p,
                           (unsigned long long *)(d_work.p + sizeof(CountWork)), false, ctx->tuned, s, nullptr);
     if (st == TC_OK && cudaEventRecord(ctx->ev[1], s) != cudaSuccess) st = set_error(TC_E_CUDA, "event record failed");
-    if (st == TC_OK && cudaMemcpyAsync(h_out.data(), d_work.p, h_out.size(), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    if (st == TC_OK && cudaMemcpyAsync(h_out, d_work.p, out_bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         st = set_error(TC_E_CUDA, "result read-back failed");
     if (st == TC_OK && cudaEventRecord(ctx->ev[2], s) != cudaSuccess) st = set_error(TC_E_CUDA, "event record failed");
     if (st == TC_OK) {
@@ -303,6 +311,8 @@ int count_graphs_direct(tc_ctx *ctx, tc_graph *const *graphs, int n, uint64_t *o
                 d_desc.release();
                 d_work.release();
                 sc = CountScratch();
+                // h_own too (the read-back may still land in it); the context's
+                // own pinned area is freed only after its stream has drained
                 return set_error(TC_E_TIMEOUT, "batched count of %d graphs did not finish in %lld ms", n,
                                  (long long)timeout_ms);
             }
@@ -310,12 +320,13 @@ int count_graphs_direct(tc_ctx *ctx, tc_graph *const *graphs, int n, uint64_t *o
         }
     }
     if (st == TC_OK) {
-        const CountWork *w = (const CountWork *)h_out.data();
+        const CountWork *w = (const CountWork *)h_out;
         if (w->error) st = set_error(TC_E_STATE, "heavy-unit list overflow");
-        else memcpy(outs, h_out.data() + sizeof(CountWork), sizeof(uint64_t) * (size_t)n);
+        else memcpy(outs, h_out + sizeof(CountWork), sizeof(uint64_t) * (size_t)n);
         if (kernel_ms) cudaEventElapsedTime(kernel_ms, ctx->ev[0], ctx->ev[1]);
     }
     scratch_free(&sc, s);
+    if (h_own) cudaFreeHost(h_own);
     return st;
 }
 

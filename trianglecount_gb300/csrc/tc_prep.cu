@@ -561,8 +561,8 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
     TC_TRY(posP.alloc((size_t)nnz + 1, s));
     TC_TRY(posH.alloc((size_t)nnz + 1, s));
     const int gV = grid(V, ctx), gE = grid(nnz, ctx);
-    int st = TC_OK;
-    for (int p = 0; p < k && st == TC_OK; ++p) {
+    // one part; any failure returns its status (the caller frees all parts)
+    auto one_part = [&](int p) -> int {
         if (V) part_flags_kernel<<<gV, 256, 0, s>>>(dpart.p, V, p, inP.p);
         TC_CUDA(cudaMemsetAsync(inH.p, 0, (size_t)V, s));
         if (nnz) halo_flags_kernel<<<gE, 256, 0, s>>>(ug->rowid, ug->col, nnz, dpart.p, p, inH.p);
@@ -653,12 +653,15 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
             out_col = col2.release();
         }
         TC_CUDA(cudaStreamSynchronize(s));
-        st = graph_adopt_device(ctx, out_rp, out_col, n_local, out_nnz, t_ver, &parts_out[p]);
-        if (st != TC_OK) {
+        const int ast = graph_adopt_device(ctx, out_rp, out_col, n_local, out_nnz, t_ver, &parts_out[p]);
+        if (ast != TC_OK) {
             dfree(out_rp, s);
             dfree(out_col, s);
         }
-    }
+        return ast;
+    };
+    int st = TC_OK;
+    for (int p = 0; p < k && st == TC_OK; ++p) st = one_part(p);
     if (st != TC_OK)
         for (int p = 0; p < k; ++p) {
             tc_graph_destroy(parts_out[p]);

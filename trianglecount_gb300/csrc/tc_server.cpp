@@ -282,13 +282,37 @@ int tc_server_submit(tc_server *s, uint64_t graph_key, const int64_t *src, const
     if (!s || !request_id || n_edges < 0 || (n_edges > 0 && (!src || !dst)))
         return set_error(TC_E_INVALID, "bad request arguments");
     Request *r = new Request();
+    r->key = graph_key;
+    r->n_nodes = n_nodes;
+    r->t_submit = Clock::now();
+    {
+        // resident key: pin the graph and go straight to the count thread,
+        // without copying the edges
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->stopping) {
+            delete r;
+            return set_error(TC_E_STATE, "server is shutting down");
+        }
+        auto it = graph_key ? s->cache.find(graph_key) : s->cache.end();
+        if (it != s->cache.end() && s->fault == TC_OK) {
+            it->second.in_use++;
+            it->second.last_use = ++s->tick;
+            r->g = it->second.g;
+            r->state = kReady;
+            r->id = s->next_id++;
+            s->reqs[r->id] = r;
+            s->ready.push_back(r);
+            s->stats.submitted++;
+            s->stats.cache_hits++;
+            *request_id = r->id;
+            s->cv.notify_all();
+            return TC_OK;
+        }
+    }
     if (n_edges > 0) {
         r->src.assign(src, src + n_edges);
         r->dst.assign(dst, dst + n_edges);
     }
-    r->key = graph_key;
-    r->n_nodes = n_nodes;
-    r->t_submit = Clock::now();
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stopping) {
         delete r;
