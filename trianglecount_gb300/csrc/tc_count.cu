@@ -99,53 +99,33 @@ __device__ __forceinline__ uint32_t table_probe(const int *tab, uint32_t mask, i
     return (uint32_t)(y == x);
 }
 
-// Cuckoo hashing (two slots per key, Pagh & Rodler; parallel insertion with
-// atomic swaps as in Alcantara et al., "Real-time parallel hashing on the
-// GPU", 2009).  A slot word holds a key in bits 0..30 and, in bit 31, a flag
-// "some key whose first slot is this one lives in its second slot".  A lookup
-// reads the key's first slot and reads the second slot only when that flag is
-// set: no loop, no divergence, and the second shared load is issued only by
-// the (few) lanes that need it, so it adds little bank traffic.  Insertion
-// places a key in its first slot, moving a displaced key to its other slot,
-// at most `kicks` times; keys only ever sit in one of their two slots and
-// flags are only ever set, so when no insertion gives up every key is found.
-// A give-up switches the task to linear probing (rebuilt), decided warp- or
-// block-uniformly.
-constexpr int kCuckooEmpty = 0x7fffffff;  // key bits all ones: no vertex id (ids < 2^31 - 1)
-constexpr int kCuckooFlag = (int)0x80000000u;
-
+// Cuckoo hashing (two slots per key, Pagh & Rodler; parallel insertion by
+// atomicExch as in Alcantara et al., "Real-time parallel hashing on the GPU",
+// 2009): a lookup reads exactly the two candidate slots -- two independent
+// shared loads, no loop, so the lanes of a warp never diverge on collisions.
+// Insertion moves a displaced key to its other slot, at most `kicks` times;
+// every key is always either in the table or in one thread's hand, so when no
+// insertion gives up, all keys are in.  A give-up switches the task to linear
+// probing (rebuilt), decided warp- or block-uniformly.
 __device__ __forceinline__ uint32_t hash_slot2(int x, int shift) { return ((uint32_t)x * 0x85EBCA77u) >> shift; }
-
-// Stores `key` in slot pos keeping the slot's flag; returns the key it displaced.
-__device__ __forceinline__ int cuckoo_place(int *tab, uint32_t pos, int key) {
-    int old = tab[pos];
-    for (;;) {
-        const int prev = atomicCAS(&tab[pos], old, key | (old & kCuckooFlag));
-        if (prev == old) return prev & ~kCuckooFlag;
-        old = prev;
-    }
-}
 
 __device__ __forceinline__ bool cuckoo_insert(int *tab, int shift, int x, int kicks) {
     int cur = x;
     uint32_t pos = hash_slot(cur, shift);
     for (int it = 0; it < kicks; ++it) {
-        const uint32_t p1 = hash_slot(cur, shift);
-        if (pos != p1) atomicOr(&tab[p1], kCuckooFlag);  // cur goes to its second slot
-        const int old = cuckoo_place(tab, pos, cur);
-        if (old == kCuckooEmpty) return true;
+        const int old = atomicExch(&tab[pos], cur);
+        if (old == kEmpty) return true;
         cur = old;
-        const uint32_t q1 = hash_slot(cur, shift), q2 = hash_slot2(cur, shift);
-        pos = pos == q1 ? q2 : q1;
+        const uint32_t p1 = hash_slot(cur, shift), p2 = hash_slot2(cur, shift);
+        pos = pos == p1 ? p2 : p1;
     }
     return false;
 }
 
 __device__ __forceinline__ uint32_t cuckoo_probe(const int *tab, int shift, int x) {
     const int a = tab[hash_slot(x, shift)];
-    bool hit = (a & ~kCuckooFlag) == x;
-    if (!hit && a < 0) hit = (tab[hash_slot2(x, shift)] & ~kCuckooFlag) == x;
-    return (uint32_t)hit;
+    const int b = tab[hash_slot2(x, shift)];
+    return (uint32_t)((a == x) | (b == x));
 }
 
 // Membership of x >= 0 in the table, by the table's mode.
@@ -156,11 +136,10 @@ __device__ __forceinline__ uint32_t probe_any(const int *tab, uint32_t mask, int
 // Table geometry for n keys: slots = max(32, next_pow2(4 n)).
 __device__ __forceinline__ int table_log_slots(int n) { return max(5, ilog2_ceil(4 * n)); }
 
-// Empties a table of (mask + 1) slots with `nthreads` threads numbered `tid`
-// (empty = -1 for linear probing, kCuckooEmpty for cuckoo); the caller
-// synchronises before inserting.
-__device__ __forceinline__ void table_clear(int *tab, uint32_t mask, int tid, int nthreads, int empty = kEmpty) {
-    for (int i = tid; i <= (int)mask; i += nthreads) tab[i] = empty;
+// Empties a table of (mask + 1) slots with `nthreads` threads numbered `tid`;
+// the caller synchronises before inserting.
+__device__ __forceinline__ void table_clear(int *tab, uint32_t mask, int tid, int nthreads) {
+    for (int i = tid; i <= (int)mask; i += nthreads) tab[i] = kEmpty;
 }
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
@@ -600,7 +579,7 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
         const uint32_t mask = (1u << lg) - 1u;
         const int shift = 32 - lg;
         if (ei != cached_entry || ti != cached_tile) {
-            table_clear(smem, mask, threadIdx.x, kThreads, P.probe_kicks > 0 ? kCuckooEmpty : kEmpty);
+            table_clear(smem, mask, threadIdx.x, kThreads);
             __syncthreads();
             bool ok = true;
             if (P.probe_kicks > 0)
@@ -675,7 +654,7 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
             const int lg = table_log_slots(T.dx);
             const uint32_t mask = (1u << lg) - 1u;
             const int shift = 32 - lg;
-            table_clear(wtab, mask, lane, kWarp, P.probe_kicks > 0 ? kCuckooEmpty : kEmpty);
+            table_clear(wtab, mask, lane, kWarp);
             __syncwarp();
             bool ok = true;
             if (P.probe_kicks > 0)
