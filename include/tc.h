@@ -79,6 +79,10 @@ TC_API int tc_ctx_destroy(tc_ctx *ctx);
 TC_API int tc_ctx_set_stream(tc_ctx *ctx, void *cuda_stream);
 TC_API void *tc_ctx_get_stream(tc_ctx *ctx);
 TC_API int tc_ctx_synchronize(tc_ctx *ctx);
+/* Device time of the count kernel alone (the persistent counting launch, not
+ * the classification passes) of the last single-graph count on this context;
+ * waits for it to finish. */
+TC_API int tc_ctx_last_count_kernel_ms(tc_ctx *ctx, float *ms);
 TC_API int tc_ctx_device_info(tc_ctx *ctx, int *sm_count, size_t *free_bytes, size_t *total_bytes);
 
 /* Strategy thresholds of the counting kernel (picked by the autotuner).

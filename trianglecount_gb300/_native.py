@@ -65,6 +65,7 @@ _SIGS = {
     "tc_ctx_set_stream": (C.c_int, [vp, vp]),
     "tc_ctx_get_stream": (vp, [vp]),
     "tc_ctx_synchronize": (C.c_int, [vp]),
+    "tc_ctx_last_count_kernel_ms": (C.c_int, [vp, P(C.c_float)]),
     "tc_ctx_device_info": (C.c_int, [vp, P(C.c_int), P(C.c_size_t), P(C.c_size_t)]),
     "tc_ctx_get_tuning": (C.c_int, [vp, P(Tuning)]),
     "tc_ctx_set_tuning": (C.c_int, [vp, P(Tuning)]),

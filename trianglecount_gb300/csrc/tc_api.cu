@@ -132,8 +132,9 @@ int enqueue_graph_count(tc_graph *g, unsigned long long *per_root, unsigned long
         g->desc_valid = true;
     }
     const int64_t chunks = (g->n_rows + 31) / 32;
+    ctx->kev_recorded = chunks > 0;
     return launch_count(g->d_desc, 1, chunks, g->n_rows + 1, g->sc, g->d_work, results ? results : g->d_result,
-                        per_root != nullptr, ctx->tuned, ctx->stream, launches);
+                        per_root != nullptr, ctx->tuned, ctx->stream, launches, ctx->kev);
 }
 
 int new_graph(tc_ctx *ctx, int64_t n_rows, int64_t nnz, int64_t n_roots, tc_graph **out) {
@@ -199,6 +200,8 @@ void ctx_release(tc_ctx *c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto &e : c->kev)
         if (e) cudaEventDestroy(e);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -413,6 +416,8 @@ int tc_ctx_create(int device, tc_ctx **out) {
     c->own_stream = true;
     for (int i = 0; i < 4 && st == TC_OK; ++i)
         if (cudaEventCreate(&c->ev[i]) != cudaSuccess) st = TC_E_CUDA;
+    for (int i = 0; i < 2 && st == TC_OK; ++i)
+        if (cudaEventCreate(&c->kev[i]) != cudaSuccess) st = TC_E_CUDA;
     if (st == TC_OK && cudaMallocHost(&c->h_pinned, 4096) != cudaSuccess) st = TC_E_CUDA;
     if (st == TC_OK) st = resolve_tuning(c->tuning, c->sm_count, &c->tuned);
     if (st != TC_OK) {
@@ -439,6 +444,14 @@ int tc_ctx_set_stream(tc_ctx *c, void *stream) {
 }
 
 void *tc_ctx_get_stream(tc_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int tc_ctx_last_count_kernel_ms(tc_ctx *c, float *ms) {
+    if (!c || !ms) return set_error(TC_E_INVALID, "null argument");
+    if (!c->kev_recorded) return set_error(TC_E_STATE, "no count kernel launched on this context yet");
+    TC_CUDA(cudaEventSynchronize(c->kev[1]));
+    TC_CUDA(cudaEventElapsedTime(ms, c->kev[0], c->kev[1]));
+    return TC_OK;
+}
 
 int tc_ctx_synchronize(tc_ctx *c) {
     if (!c) return set_error(TC_E_INVALID, "null context");

@@ -720,7 +720,7 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
 
 int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, int64_t total_vertices,
                  const CountScratch &sc, CountWork *work, unsigned long long *results, bool per_root, const Tuned &tn,
-                 cudaStream_t s, int *launches) {
+                 cudaStream_t s, int *launches, cudaEvent_t *kev) {
     KParams P;
     P.gd = d_desc;
     P.n_graphs = n_graphs;
@@ -757,13 +757,12 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
         TC_TRY(scan_exclusive_i32(sc.in_cnt, sc.in_off, total_vertices, s));
         transpose_classify_kernel<<<aux_blocks, kThreads, 0, s>>>(P, sc.heavy);
         TC_CUDA(cudaGetLastError());
-        if (per_root) {
-            micro_kernel<true><<<aux_blocks, kThreads, 0, s>>>(P);
-            count_kernel<true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
-        } else {
-            micro_kernel<false><<<aux_blocks, kThreads, 0, s>>>(P);
-            count_kernel<false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
-        }
+        if (per_root) micro_kernel<true><<<aux_blocks, kThreads, 0, s>>>(P);
+        else micro_kernel<false><<<aux_blocks, kThreads, 0, s>>>(P);
+        if (kev) TC_CUDA(cudaEventRecord(kev[0], s));
+        if (per_root) count_kernel<true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        else count_kernel<false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        if (kev) TC_CUDA(cudaEventRecord(kev[1], s));
         TC_CUDA(cudaGetLastError());
         nl = 4 + (total_vertices > 4096 ? 3 : 1);
     }

@@ -129,9 +129,10 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
 // results[n_graphs] receives the per-graph totals (zeroed here).
 // Enqueues [in_count -> scan -> transpose/classify -> count] for n_graphs
 // descriptors on stream s; total_vertices = sum (n_rows + 1).
+// kev (optional, two events) is recorded around the count kernel alone.
 int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, int64_t total_vertices,
                  const CountScratch &sc, CountWork *work, unsigned long long *results, bool per_root, const Tuned &tn,
-                 cudaStream_t s, int *launches);
+                 cudaStream_t s, int *launches, cudaEvent_t *kev = nullptr);
 
 // ---- scans and sort (tc_scan.cu, tc_sort.cu) ----------------------------------------
 // Exclusive scan of n values into out[0..n] (out[n] = total).  out may alias in.
@@ -175,6 +176,8 @@ struct tc_ctx {
     tc_tuning tuning{};
     tc::Tuned tuned{};
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t kev[2] = {nullptr, nullptr};  // around the last count kernel launch
+    bool kev_recorded = false;
     unsigned long long *h_pinned = nullptr;  // small pinned read-back area
     std::atomic<int> refs{1};                // the handle + one per live object
 };
