@@ -95,7 +95,10 @@ TC_API int tc_ctx_device_info(tc_ctx *ctx, int *sm_count, size_t *free_bytes, si
  * across the lanes.  probe_kicks > 0 selects a cuckoo hash (two fixed probe
  * slots per lookup, at most probe_kicks displacements per insertion, falling
  * back to linear probing for a task whose insertion gives up); 0 selects
- * linear probing.  In tc_ctx_set_tuning, fields <= 0 (long_list, probe_kicks,
+ * linear probing.  heavy_bitmap = 1 runs heavy tasks on a direct-address
+ * shared-memory bitmap of N+(x) (one load per probe) whenever the graphs'
+ * vertex ids fit in one block's shared memory (about 1.85 M rows).  In
+ * tc_ctx_set_tuning, fields <= 0 (long_list, probe_kicks, heavy_bitmap,
  * blocks_per_sm: < 0) keep the current value. */
 typedef struct tc_tuning {
     int32_t warp_max_deg;   /* 32..512, power of two */
@@ -103,6 +106,7 @@ typedef struct tc_tuning {
     int32_t unit_work;      /* target wedge probes per heavy block unit */
     int32_t long_list;      /* 0..4096 */
     int32_t probe_kicks;    /* 0..1024 */
+    int32_t heavy_bitmap;   /* 0 or 1 */
     int32_t blocks_per_sm;  /* persistent grid = SMs * this (0: occupancy) */
 } tc_tuning;
 TC_API int tc_ctx_get_tuning(tc_ctx *ctx, tc_tuning *out);

@@ -18,7 +18,10 @@ TUNINGS = [
     {"warp_max_deg": 512, "light_max_work": 1 << 30, "unit_work": 1 << 30, "long_list": 4096,
      "probe_kicks": 0},  # warps only, flattened, linear probing
     {"warp_max_deg": 64, "light_max_work": 500, "unit_work": 3000, "long_list": 5, "blocks_per_sm": 1},
-    {"probe_kicks": 1},  # cuckoo insertions give up often: exercises the linear-probing fallback
+    {"probe_kicks": 1, "heavy_bitmap": 0},  # cuckoo give-ups: exercises the linear-probing fallback
+    {"heavy_bitmap": 0, "warp_max_deg": 32, "light_max_work": 64},  # heavy work on shared hash tiles
+    {"heavy_bitmap": 1, "warp_max_deg": 32, "light_max_work": 64},  # heavy work on the id bitmap kernel
+    {"heavy_bitmap": 1},
 ]
 
 
@@ -27,7 +30,7 @@ def tuned(ctx):
     old = ctx.get_tuning()
     yield ctx
     ctx.set_tuning(old["warp_max_deg"], old["light_max_work"], old["unit_work"], old["long_list"],
-                   old["probe_kicks"], 0)
+                   old["probe_kicks"], old["heavy_bitmap"], 0)
 
 
 @pytest.mark.parametrize("tuning", TUNINGS)

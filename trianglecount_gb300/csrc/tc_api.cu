@@ -133,8 +133,9 @@ int enqueue_graph_count(tc_graph *g, unsigned long long *per_root, unsigned long
     }
     const int64_t chunks = (g->n_rows + 31) / 32;
     ctx->kev_recorded = chunks > 0;
-    return launch_count(g->d_desc, 1, chunks, g->n_rows + 1, g->sc, g->d_work, results ? results : g->d_result,
-                        per_root != nullptr, ctx->tuned, ctx->stream, launches, ctx->kev);
+    return launch_count(g->d_desc, 1, chunks, g->n_rows + 1, g->n_rows, g->sc, g->d_work,
+                        results ? results : g->d_result, per_root != nullptr, ctx->tuned, ctx->stream, launches,
+                        ctx->kev);
 }
 
 int new_graph(tc_ctx *ctx, int64_t n_rows, int64_t nnz, int64_t n_roots, tc_graph **out) {
@@ -257,9 +258,10 @@ int count_graphs_direct(tc_ctx *ctx, tc_graph *const *graphs, int n, uint64_t *o
     if (!ctx || n <= 0 || !graphs || !outs) return set_error(TC_E_INVALID, "bad batch arguments");
     cudaStream_t s = ctx->stream;
     std::vector<GraphDesc> desc((size_t)n);
-    int64_t chunks = 0, cap = 0, vtot = 0, etot = 0;
+    int64_t chunks = 0, cap = 0, vtot = 0, etot = 0, max_rows = 0;
     for (int i = 0; i < n; ++i) {
         const tc_graph *g = graphs[i];
+        if (g) max_rows = std::max(max_rows, g->n_rows);
         if (!g || g->ctx->device != ctx->device) return set_error(TC_E_INVALID, "graph %d is null or on another device", i);
         memset(&desc[(size_t)i], 0, sizeof(GraphDesc));
         desc[(size_t)i].rp = g->rp;
@@ -293,7 +295,7 @@ int count_graphs_direct(tc_ctx *ctx, tc_graph *const *graphs, int n, uint64_t *o
         st = set_error(TC_E_CUDA, "descriptor upload failed");
     if (st == TC_OK && cudaEventRecord(ctx->ev[0], s) != cudaSuccess) st = set_error(TC_E_CUDA, "event record failed");
     if (st == TC_OK)
-        st = launch_count(d_desc.p, n, chunks, vtot, sc, (CountWork *)d_work.p,
+        st = launch_count(d_desc.p, n, chunks, vtot, max_rows, sc, (CountWork *)d_work.p,
                           (unsigned long long *)(d_work.p + sizeof(CountWork)), false, ctx->tuned, s, nullptr);
     if (st == TC_OK && cudaEventRecord(ctx->ev[1], s) != cudaSuccess) st = set_error(TC_E_CUDA, "event record failed");
     if (st == TC_OK && cudaMemcpyAsync(h_out, d_work.p, out_bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess)
@@ -392,6 +394,7 @@ int tc_host_free_pinned(void *p) {
 
 int tc_ctx_create(int device, tc_ctx **out) {
     if (!out) return set_error(TC_E_INVALID, "null output");
+    g_last_error.clear();
     *out = nullptr;
     int n = 0;
     cudaError_t e = cudaGetDeviceCount(&n);
@@ -410,6 +413,7 @@ int tc_ctx_create(int device, tc_ctx **out) {
     c->tuning.unit_work = 262144;
     c->tuning.long_list = 32;
     c->tuning.probe_kicks = 32;
+    c->tuning.heavy_bitmap = 0;  // an autotuner candidate: one 32-warp block per SM rarely pays off
     c->tuning.blocks_per_sm = 0;
     int st = TC_OK;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) st = TC_E_CUDA;
@@ -421,7 +425,8 @@ int tc_ctx_create(int device, tc_ctx **out) {
     if (st == TC_OK && cudaMallocHost(&c->h_pinned, 4096) != cudaSuccess) st = TC_E_CUDA;
     if (st == TC_OK) st = resolve_tuning(c->tuning, c->sm_count, &c->tuned);
     if (st != TC_OK) {
-        if (st == TC_E_CUDA) set_error(st, "context creation failed on device %d", device);
+        const std::string why = tc_last_error();
+        set_error(st, "context creation failed on device %d: %s", device, why.empty() ? "CUDA error" : why.c_str());
         tc_ctx_destroy(c);
         return st;
     }
@@ -485,6 +490,7 @@ int tc_ctx_set_tuning(tc_ctx *c, const tc_tuning *in) {
     if (in->unit_work > 0) t.unit_work = in->unit_work;
     if (in->long_list >= 0) t.long_list = in->long_list;
     if (in->probe_kicks >= 0) t.probe_kicks = in->probe_kicks;
+    if (in->heavy_bitmap >= 0) t.heavy_bitmap = in->heavy_bitmap;
     if (in->blocks_per_sm >= 0) t.blocks_per_sm = in->blocks_per_sm;
     Tuned r;
     TC_TRY(resolve_tuning(t, c->sm_count, &r));
@@ -722,9 +728,10 @@ int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out)
     b->n = n;
     cudaStream_t s = ctx->stream;
     std::vector<GraphDesc> desc((size_t)n);
-    int64_t chunks = 0, cap = 0, vtot = 0, etot = 0;
+    int64_t chunks = 0, cap = 0, vtot = 0, etot = 0, max_rows = 0;
     for (int i = 0; i < n; ++i) {
         tc_graph *g = graphs[i];
+        if (g) max_rows = std::max(max_rows, g->n_rows);
         if (!g || g->ctx != ctx) {
             tc_batch_destroy(b);
             return set_error(TC_E_INVALID, "graph %d is null or belongs to another context", i);
@@ -758,8 +765,8 @@ int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out)
     if (st == TC_OK && cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         st = set_error(TC_E_CUDA, "stream capture could not start");
     if (st == TC_OK) {
-        int ls = launch_count(b->d_desc, n, chunks, vtot, b->sc, b->d_work, (unsigned long long *)(b->d_work + 1),
-                              false, ctx->tuned, s, nullptr);
+        int ls = launch_count(b->d_desc, n, chunks, vtot, max_rows, b->sc, b->d_work,
+                              (unsigned long long *)(b->d_work + 1), false, ctx->tuned, s, nullptr);
         cudaError_t e = cudaStreamEndCapture(s, &b->graph);
         if (ls != TC_OK) st = ls;
         else if (e != cudaSuccess) st = cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);

@@ -128,6 +128,14 @@ __device__ __forceinline__ uint32_t cuckoo_probe(const int *tab, int shift, int 
     return (uint32_t)((a == x) | (b == x));
 }
 
+// Membership of x in a direct-address bitmap of vertex ids (bit x of word
+// x/32).  A negative x (a padding lane) reads word 0 and reports no hit, so
+// the load stays inside the bitmap.
+__device__ __forceinline__ uint32_t bitmap_probe(const int *bm, int x) {
+    const int y = x < 0 ? 0 : x;
+    return ((uint32_t)bm[(unsigned)y >> 5] >> (y & 31)) & (uint32_t)(x >= 0);
+}
+
 // Membership of x >= 0 in the table, by the table's mode.
 __device__ __forceinline__ uint32_t probe_any(const int *tab, uint32_t mask, int shift, int x, bool cuckoo) {
     return cuckoo ? cuckoo_probe(tab, shift, x) : table_probe(tab, mask, shift, x);
@@ -180,6 +188,7 @@ struct KParams {
     int tile;
     int long_list;
     int probe_kicks;  // 0: linear probing; > 0: cuckoo with this many kicks
+    int heavy_done;   // heavy units belong to heavy_bitmap_kernel: count_kernel skips phase A
 };
 
 // Where the partner p_j of task x lives and whose root it credits.
@@ -196,7 +205,7 @@ struct Task {
 // out-neighbours v of x, skipped unless d+(v) <= d+(x); the others are
 // in-neighbours u.  Returns this lane's hit count; with per_root set, hits are
 // also credited to their root (x for out-partners, u for in-partners).
-template <bool kPerRoot>
+template <bool kPerRoot, bool kBitmap = false>
 __device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
                                                    const Task &T, int j0, int j1, const int *tab, uint32_t mask,
                                                    int shift, bool cuckoo, int long_list, int lane,
@@ -232,7 +241,10 @@ __device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ r
                 const int t = base + i * kWarp + lane;
                 x[i] = t < ll ? __ldg(p + t) : -1;
             }
-            if (cuckoo) {
+            if (kBitmap) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) h += (uint32_t)(x[i] >= 0) & bitmap_probe(tab, x[i]);
+            } else if (cuckoo) {
 #pragma unroll
                 for (int i = 0; i < 4; ++i) h += (uint32_t)(x[i] >= 0) & cuckoo_probe(tab, shift, x[i]);
             } else {
@@ -271,7 +283,8 @@ __device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ r
         const int s_seg = __shfl_sync(kFull, s2, seg);
         const int own = kPerRoot ? __shfl_sync(kFull, owner, seg) : 0;
         if (t < total) {
-            const uint32_t h = probe_any(tab, mask, shift, __ldg(col + s_seg + (t - ex_seg)), cuckoo);
+            const int y = __ldg(col + s_seg + (t - ex_seg));
+            const uint32_t h = kBitmap ? bitmap_probe(tab, y) : probe_any(tab, mask, shift, y, cuckoo);
             hits += h;
             if (kPerRoot && h) atomicAdd(per_root + own, 1ull);
         }
@@ -500,6 +513,119 @@ __global__ void __launch_bounds__(kThreads) micro_kernel(KParams P) {
     }
 }
 
+// Heavy units with a direct-address bitmap of N+(x) over all vertex ids in
+// shared memory (graphs of at most bitmap_words * 32 rows): one shared load per
+// probe instead of the two of the cuckoo hash, and no tiling of N+(x).  One
+// kBigThreads block per SM drains the heavy-unit cursor before count_kernel
+// runs (which then finds no heavy units left).  Bits are set for the unit's
+// N+(x) and cleared again (their words zeroed) when the next unit needs
+// another set.
+constexpr int kBigThreads = 1024;
+
+template <bool kPerRoot>
+__global__ void __launch_bounds__(kBigThreads, 1) heavy_bitmap_kernel(KParams P, int bitmap_words) {
+    extern __shared__ int bm[];
+    __shared__ unsigned s_unit;
+    __shared__ int s_entry;
+    __shared__ int s_chunk;
+    const int lane = threadIdx.x & (kWarp - 1);
+    const int warp = threadIdx.x / kWarp;
+    if (P.work->error) return;
+    const unsigned long long packed = P.work->heavy_packed;
+    const unsigned n_entries = (unsigned)min((unsigned long long)(packed >> 32), (unsigned long long)P.heavy_cap);
+    const unsigned n_units = (unsigned)(packed & 0xffffffffull);
+    if (n_units == 0) return;
+    for (int i = threadIdx.x; i < bitmap_words; i += kBigThreads) bm[i] = 0;
+    unsigned long long acc = 0;
+    int cur_g = -1;
+    int set_entry = -1;  // entry whose N+(x) bits are set
+    const int32_t *set_list = nullptr;
+    int set_len = 0;
+    for (;;) {
+        if (warp == 0) {
+            unsigned unit = 0;
+            if (lane == 0) unit = atomicAdd(&P.work->heavy_cursor, 1u);
+            unit = __shfl_sync(kFull, unit, 0);
+            int e = -1;
+            if (unit < n_units && n_entries > 0) {
+                int lo = 0, hi = (int)n_entries;
+                while (hi - lo > kWarp) {
+                    const int step = (hi - lo + kWarp - 1) / kWarp;
+                    const int idx = lo + lane * step;
+                    const bool le = idx < hi && (unsigned)P.heavy[idx].unit_base <= unit;
+                    const unsigned m = __ballot_sync(kFull, le);
+                    lo += (31 - __clz(m)) * step;
+                    hi = min(hi, lo + step);
+                }
+                const bool le = lo + lane < hi && (unsigned)P.heavy[lo + lane].unit_base <= unit;
+                e = lo + 31 - __clz(__ballot_sync(kFull, le));
+            }
+            if (lane == 0) {
+                s_unit = unit;
+                s_entry = e;
+                s_chunk = 0;
+            }
+        }
+        __syncthreads();
+        const unsigned unit = s_unit;
+        const int ei = s_entry;
+        if (ei < 0) break;
+        const HeavyEntry e = P.heavy[ei];
+        const GraphDesc &G = P.gd[e.g];
+        const int32_t *__restrict__ rp = G.rp;
+        const int32_t *__restrict__ col = G.col;
+        Task T;
+        const int rs = __ldg(rp + e.u);
+        T.dx = __ldg(rp + e.u + 1) - rs;
+        T.x = e.u;
+        T.n_out = e.u < G.n_roots ? T.dx : 0;
+        T.out_nbr = col + rs;
+        const int in0 = P.in_off[G.vbase + e.u];
+        T.in_nbr = P.in_list + in0;
+        const int n_part = T.n_out + (P.in_off[G.vbase + e.u + 1] - in0);
+        if (ei != set_entry) {
+            for (int i = threadIdx.x; i < set_len; i += kBigThreads) bm[(unsigned)__ldg(set_list + i) >> 5] = 0;
+            __syncthreads();
+            for (int i = threadIdx.x; i < T.dx; i += kBigThreads) {
+                const int y = __ldg(col + rs + i);
+                atomicOr(&bm[(unsigned)y >> 5], 1 << (y & 31));
+            }
+            set_entry = ei;
+            set_list = col + rs;
+            set_len = T.dx;
+        }
+        __syncthreads();
+        const int ns = e.n_slices;
+        const int si = (int)(unit - (unsigned)e.unit_base);
+        const int per = (n_part + ns - 1) / ns;
+        const int j0 = si * per, j1 = min(n_part, j0 + per);
+        uint32_t hits = 0;
+        for (;;) {
+            int c = 0;
+            if (lane == 0) c = atomicAdd(&s_chunk, 1);
+            c = __shfl_sync(kFull, c, 0);
+            const int jb = j0 + c * kHeavyChunk;
+            if (jb >= j1) break;
+            hits += probe_partners<kPerRoot, true>(rp, col, T, jb, min(jb + kHeavyChunk, j1), bm, 0, 0, false,
+                                                   P.long_list, lane, G.per_root);
+        }
+        if (!kPerRoot) {
+            if (e.g != cur_g) {
+                const unsigned long long s = warp_sum_u64(acc);
+                if (lane == 0 && cur_g >= 0 && s) atomicAdd(P.results + cur_g, s);
+                acc = 0;
+                cur_g = e.g;
+            }
+            acc += hits;
+        }
+        __syncthreads();
+    }
+    if (!kPerRoot) {
+        const unsigned long long s = warp_sum_u64(acc);
+        if (lane == 0 && cur_g >= 0 && s) atomicAdd(P.results + cur_g, s);
+    }
+}
+
 template <bool kPerRoot>
 __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KParams P) {
     extern __shared__ int smem[];
@@ -526,7 +652,7 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
     // ---- phase A: heavy units, one block each ----
     int cached_entry = -1, cached_tile = -1;
     bool cached_cuckoo = false;
-    for (;;) {
+    for (; !P.heavy_done;) {
         if (warp == 0) {
             unsigned unit = 0;
             if (lane == 0) unit = atomicAdd(&P.work->heavy_cursor, 1u);
@@ -703,6 +829,21 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     r.unit_work = t.unit_work > 0 ? t.unit_work : 262144;
     r.long_list = t.long_list >= 0 ? t.long_list : 32;
     r.probe_kicks = t.probe_kicks >= 0 ? t.probe_kicks : 32;
+    r.heavy_bitmap = t.heavy_bitmap >= 0 ? t.heavy_bitmap : 0;
+    r.sm_count = sm_count;
+    {
+        // the bitmap takes what one block may opt into, minus the kernel's static shared memory
+        int dev = 0, optin = 0;
+        TC_CUDA(cudaGetDevice(&dev));
+        TC_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        cudaFuncAttributes fa;
+        TC_CUDA(cudaFuncGetAttributes(&fa, heavy_bitmap_kernel<true>));
+        r.bitmap_bytes = std::max(0, (optin - (int)fa.sharedSizeBytes - 256) & ~255);
+        TC_CUDA(cudaFuncSetAttribute(heavy_bitmap_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     r.bitmap_bytes));
+        TC_CUDA(cudaFuncSetAttribute(heavy_bitmap_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     r.bitmap_bytes));
+    }
     if (r.probe_kicks > 1024) return set_error(TC_E_INVALID, "probe_kicks must be <= 1024, got %d", r.probe_kicks);
     if (r.long_list > 4096) return set_error(TC_E_INVALID, "long_list must be <= 4096, got %d", r.long_list);
     r.threads = kThreads;
@@ -719,8 +860,8 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
 }
 
 int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, int64_t total_vertices,
-                 const CountScratch &sc, CountWork *work, unsigned long long *results, bool per_root, const Tuned &tn,
-                 cudaStream_t s, int *launches, cudaEvent_t *kev) {
+                 int64_t max_rows, const CountScratch &sc, CountWork *work, unsigned long long *results, bool per_root,
+                 const Tuned &tn, cudaStream_t s, int *launches, cudaEvent_t *kev) {
     KParams P;
     P.gd = d_desc;
     P.n_graphs = n_graphs;
@@ -743,6 +884,11 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
     P.tile = tn.tile;
     P.long_list = tn.long_list;
     P.probe_kicks = tn.probe_kicks;
+    // heavy units on direct-address bitmaps when every graph's ids fit in shared memory
+    const int64_t bitmap_words = (max_rows + 31) / 32;
+    const bool bitmap = tn.heavy_bitmap && bitmap_words > 0 && bitmap_words * 4 <= (int64_t)tn.bitmap_bytes;
+    P.heavy_done = bitmap ? 1 : 0;
+    if (bitmap) P.tile = INT32_MAX / 2;  // one tile: the bitmap has no capacity limit
     TC_CUDA(cudaMemsetAsync(work, 0, sizeof(CountWork), s));
     TC_CUDA(cudaMemsetAsync(results, 0, sizeof(unsigned long long) * (size_t)n_graphs, s));
     int nl = 0;
@@ -760,11 +906,18 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
         if (per_root) micro_kernel<true><<<aux_blocks, kThreads, 0, s>>>(P);
         else micro_kernel<false><<<aux_blocks, kThreads, 0, s>>>(P);
         if (kev) TC_CUDA(cudaEventRecord(kev[0], s));
+        if (bitmap) {
+            const size_t bytes = (size_t)bitmap_words * 4;
+            if (per_root) heavy_bitmap_kernel<true><<<tn.sm_count, kBigThreads, bytes, s>>>(P, (int)bitmap_words);
+            else heavy_bitmap_kernel<false><<<tn.sm_count, kBigThreads, bytes, s>>>(P, (int)bitmap_words);
+            TC_CUDA(cudaGetLastError());
+            ++nl;
+        }
         if (per_root) count_kernel<true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
         else count_kernel<false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
         if (kev) TC_CUDA(cudaEventRecord(kev[1], s));
         TC_CUDA(cudaGetLastError());
-        nl = 4 + (total_vertices > 4096 ? 3 : 1);
+        nl += 4 + (total_vertices > 4096 ? 3 : 1);
     }
     if (launches) *launches = nl;
     return TC_OK;
@@ -795,6 +948,7 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
     P.tile = tn.tile;
     P.long_list = tn.long_list;
     P.probe_kicks = tn.probe_kicks;
+    P.heavy_done = 0;
     TC_CUDA(cudaMemsetAsync(work, 0, sizeof(CountWork), s));
     TC_CUDA(cudaMemsetAsync(results, 0, sizeof(unsigned long long), s));
     if (total_chunks > 0) {

@@ -110,6 +110,9 @@ struct Tuned {  // resolved tc_tuning with derived table geometry
     int unit_work;
     int long_list;
     int probe_kicks;     // 0: linear-probing hash; > 0: cuckoo hash with this kick bound
+    int heavy_bitmap;    // 1: heavy units on direct-address bitmaps when the ids fit
+    int bitmap_bytes;    // shared memory the bitmap kernel may use (ids < 8 x this)
+    int sm_count;
     int tile;            // block table entries per tile (a quarter of its slots)
     int log_block_slots;
     int threads;         // per block
@@ -129,10 +132,11 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
 // results[n_graphs] receives the per-graph totals (zeroed here).
 // Enqueues [in_count -> scan -> transpose/classify -> count] for n_graphs
 // descriptors on stream s; total_vertices = sum (n_rows + 1).
-// kev (optional, two events) is recorded around the count kernel alone.
+// max_rows = largest n_rows among the graphs.  kev (optional, two events) is
+// recorded around the counting kernels (heavy bitmap + persistent count).
 int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, int64_t total_vertices,
-                 const CountScratch &sc, CountWork *work, unsigned long long *results, bool per_root, const Tuned &tn,
-                 cudaStream_t s, int *launches, cudaEvent_t *kev = nullptr);
+                 int64_t max_rows, const CountScratch &sc, CountWork *work, unsigned long long *results, bool per_root,
+                 const Tuned &tn, cudaStream_t s, int *launches, cudaEvent_t *kev = nullptr);
 
 // ---- scans and sort (tc_scan.cu, tc_sort.cu) ----------------------------------------
 // Exclusive scan of n values into out[0..n] (out[n] = total).  out may alias in.

@@ -73,6 +73,7 @@ int setup_device(int dev, DeviceSetup **out) {
         t.unit_work = 262144;
         t.long_list = 32;
         t.probe_kicks = 32;
+        t.heavy_bitmap = 0;  // the allocation-free variant keeps the fixed heavy path
         t.blocks_per_sm = 0;
         TC_TRY(resolve_tuning(t, device_sm_count(dev), &d.tuned));
         d.scratch = (unsigned char *)p;

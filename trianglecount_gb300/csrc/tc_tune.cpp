@@ -43,17 +43,18 @@ extern "C" int tc_autotune(tc_ctx *ctx, tc_graph *g, int max_trials, int reps, t
     float cur_ms = 0;
     TC_TRY(time_count(ctx, g, reps, &cur_ms));
     int trials = 1;
-    const std::vector<int32_t> grid[5] = {
+    const std::vector<int32_t> grid[6] = {
         {64, 128, 256, 512},
         {4096, 8192, 16384, 32768, 65536, 131072},
         {65536, 131072, 262144, 524288, 1048576},
         {8, 16, 32, 64},
         {0, 32},
+        {0, 1},
     };
     bool changed = true;
     while (changed && trials < max_trials) {
         changed = false;
-        for (int p = 0; p < 5 && trials < max_trials; ++p) {
+        for (int p = 0; p < 6 && trials < max_trials; ++p) {
             for (int32_t v : grid[p]) {
                 if (trials >= max_trials) break;
                 tc_tuning t = cur;
@@ -61,7 +62,8 @@ extern "C" int tc_autotune(tc_ctx *ctx, tc_graph *g, int max_trials, int reps, t
                                  : p == 1 ? &t.light_max_work
                                  : p == 2 ? &t.unit_work
                                  : p == 3 ? &t.long_list
-                                          : &t.probe_kicks;
+                                 : p == 4 ? &t.probe_kicks
+                                          : &t.heavy_bitmap;
                 if (*field == v) continue;
                 *field = v;
                 TC_TRY(tc_ctx_set_tuning(ctx, &t));
