@@ -219,6 +219,7 @@ int scratch_alloc(CountScratch *sc, int64_t V, int64_t C, int64_t E, int64_t hea
     TC_TRY(dalloc((void **)&sc->in_work, sizeof(unsigned long long) * (size_t)std::max<int64_t>(V, 1), s));
     TC_TRY(dalloc((void **)&sc->out_work, sizeof(unsigned long long) * (size_t)std::max<int64_t>(V, 1), s));
     TC_TRY(dalloc((void **)&sc->in_list, sizeof(int32_t) * (size_t)std::max<int64_t>(E, 1), s));
+    TC_TRY(dalloc((void **)&sc->mid, (size_t)std::max<int64_t>(E, 1), s));
     return TC_OK;
 }
 
@@ -231,6 +232,7 @@ void scratch_free(CountScratch *sc, cudaStream_t s) {
     dfree(sc->in_work, s);
     dfree(sc->out_work, s);
     dfree(sc->in_list, s);
+    dfree(sc->mid, s);
     *sc = CountScratch();
 }
 
@@ -249,7 +251,7 @@ int graph_rebind(tc_graph *g, tc_ctx *ctx) {
 
 size_t graph_device_bytes(const tc_graph *g) {
     const size_t csr = sizeof(int32_t) * (size_t)(g->n_rows + 1 + g->nnz);
-    const size_t scratch = (size_t)(g->n_rows + 1) * (4 + 4 + 8 + 8 + 16 + 1) + (size_t)g->nnz * 4 + 1024;
+    const size_t scratch = (size_t)(g->n_rows + 1) * (4 + 4 + 8 + 8 + 16 + 1) + (size_t)g->nnz * 5 + 1024;
     return csr + scratch;
 }
 
@@ -270,6 +272,7 @@ int count_graphs_direct(tc_ctx *ctx, tc_graph *const *graphs, int n, uint64_t *o
         desc[(size_t)i].n_roots = g->n_roots;
         desc[(size_t)i].chunk_base = chunks;
         desc[(size_t)i].vbase = vtot;
+        desc[(size_t)i].ebase = etot;
         chunks += (g->n_rows + 31) / 32;
         vtot += g->n_rows + 1;
         etot += g->nnz;
@@ -744,6 +747,7 @@ int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out)
         desc[i].n_roots = g->n_roots;
         desc[i].chunk_base = chunks;
         desc[i].vbase = vtot;
+        desc[i].ebase = etot;
         desc[i].per_root = nullptr;
         chunks += (g->n_rows + 31) / 32;
         vtot += g->n_rows + 1;

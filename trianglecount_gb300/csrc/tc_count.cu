@@ -181,6 +181,7 @@ struct KParams {
     unsigned long long *in_work;   // per vertex: sum of d+(u) over its in-partners u
     unsigned long long *out_work;  // per vertex: sum of d+(v) over its out-partners v
     int32_t *in_list;      // in-partner lists, in_off-indexed
+    uint8_t *mid;          // per oriented edge (pooled by ebase): 1 = middle-centric
     int warp_max;
     int log_warp_slots;
     int light_max_work;
@@ -310,17 +311,26 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
             rs = __ldg(rp + x0 + lane);
             d = __ldg(rp + x0 + lane + 1) - rs;
         }
-        // short rows: one per lane
+        // short rows: one per lane, four edges' loads in flight at a time
         if (d >= 1 && d <= kLaneRowDeg) {
             unsigned long long ow = 0;
-            for (int i = 0; i < d; ++i) {
-                const int v = __ldg(col + rs + i);
-                const int dv = __ldg(rp + v + 1) - __ldg(rp + v);
-                if (d < dv) {
-                    atomicAdd(P.in_cnt + G.vbase + v, 1);
-                    atomicAdd(P.in_work + G.vbase + v, (unsigned long long)d);
-                } else {
-                    ow += (unsigned long long)dv;
+            for (int i0 = 0; i0 < d; i0 += 4) {
+                int v[4], dv[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) v[q] = i0 + q < d ? __ldg(col + rs + i0 + q) : -1;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) dv[q] = v[q] >= 0 ? __ldg(rp + v[q] + 1) - __ldg(rp + v[q]) : 0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (v[q] < 0) continue;
+                    const bool m = d < dv[q];
+                    P.mid[G.ebase + rs + i0 + q] = (uint8_t)m;
+                    if (m) {
+                        atomicAdd(P.in_cnt + G.vbase + v[q], 1);
+                        atomicAdd(P.in_work + G.vbase + v[q], (unsigned long long)d);
+                    } else {
+                        ow += (unsigned long long)dv[q];
+                    }
                 }
             }
             P.out_work[G.vbase + x0 + lane] = ow;
@@ -336,7 +346,9 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
             for (int i = lane; i < rd; i += kWarp) {
                 const int v = __ldg(col + rrs + i);
                 const int dv = __ldg(rp + v + 1) - __ldg(rp + v);
-                if (rd < dv) {
+                const bool m = rd < dv;
+                P.mid[G.ebase + rrs + i] = (uint8_t)m;
+                if (m) {
                     atomicAdd(P.in_cnt + G.vbase + v, 1);
                     atomicAdd(P.in_work + G.vbase + v, (unsigned long long)rd);
                 } else {
@@ -371,15 +383,14 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
             nin = P.in_off[G.vbase + x + 1] - P.in_off[G.vbase + x];
             w = P.out_work[G.vbase + x] + P.in_work[G.vbase + x];
         }
-        // scatter the middle-centric out-edges of the chunk's roots: short rows one per lane ...
+        // scatter the middle-centric out-edges of the chunk's roots (marked by
+        // in_count): short rows one per lane ...
         if (d >= 1 && d <= kLaneRowDeg && x < G.n_roots) {
             for (int i = 0; i < d; ++i) {
+                if (!P.mid[G.ebase + rs + i]) continue;
                 const int v = __ldg(col + rs + i);
-                const int dv = __ldg(rp + v + 1) - __ldg(rp + v);
-                if (d < dv) {
-                    const int pos = atomicSub(P.in_cnt + G.vbase + v, 1) - 1;
-                    P.in_list[P.in_off[G.vbase + v] + pos] = (int32_t)x;
-                }
+                const int pos = atomicSub(P.in_cnt + G.vbase + v, 1) - 1;
+                P.in_list[P.in_off[G.vbase + v] + pos] = (int32_t)x;
             }
         }
         // ... long rows by the whole warp
@@ -390,12 +401,10 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
             const int rrs = __shfl_sync(kFull, rs, k);
             const int rd = __shfl_sync(kFull, d, k);
             for (int i = lane; i < rd; i += kWarp) {
+                if (!P.mid[G.ebase + rrs + i]) continue;
                 const int v = __ldg(col + rrs + i);
-                const int dv = __ldg(rp + v + 1) - __ldg(rp + v);
-                if (rd < dv) {
-                    const int pos = atomicSub(P.in_cnt + G.vbase + v, 1) - 1;
-                    P.in_list[P.in_off[G.vbase + v] + pos] = (int32_t)(x0 + k);
-                }
+                const int pos = atomicSub(P.in_cnt + G.vbase + v, 1) - 1;
+                P.in_list[P.in_off[G.vbase + v] + pos] = (int32_t)(x0 + k);
             }
         }
         // classify
@@ -877,6 +886,7 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
     P.in_work = sc.in_work;
     P.out_work = sc.out_work;
     P.in_list = sc.in_list;
+    P.mid = sc.mid;
     P.warp_max = tn.warp_max;
     P.log_warp_slots = tn.log_warp_slots;
     P.light_max_work = tn.light_max_work;
@@ -941,6 +951,7 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
     P.in_work = sc.in_work;
     P.out_work = sc.out_work;
     P.in_list = sc.in_list;
+    P.mid = sc.mid;
     P.warp_max = tn.warp_max;
     P.log_warp_slots = tn.log_warp_slots;
     P.light_max_work = tn.light_max_work;

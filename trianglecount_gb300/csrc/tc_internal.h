@@ -71,6 +71,7 @@ struct GraphDesc {
     int64_t n_roots;
     int64_t chunk_base;           // exclusive prefix of 32-row chunks over graphs
     int64_t vbase;                // exclusive prefix of (n_rows + 1) over graphs
+    int64_t ebase;                // exclusive prefix of nnz over graphs
     unsigned long long *per_root; // optional g_sum output (zeroed by the caller)
 };
 
@@ -90,6 +91,7 @@ struct CountScratch {
     unsigned long long *in_work = nullptr;  // V
     unsigned long long *out_work = nullptr; // V
     int32_t *in_list = nullptr;             // E
+    uint8_t *mid = nullptr;                 // E: edge done middle-centric
 };
 int scratch_alloc(CountScratch *sc, int64_t V, int64_t C, int64_t E, int64_t heavy_cap, cudaStream_t s);
 void scratch_free(CountScratch *sc, cudaStream_t s);

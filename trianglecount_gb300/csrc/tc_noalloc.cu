@@ -7,7 +7,7 @@
 // host denies allocations.  tc_count_noalloc_i32 serves them: the caller hands
 // in device pointers to the oriented CSR and to the 8-byte result, and every
 // scratch array the count needs lives in one file-scope device array of fixed
-// size (kScratchBytes below, about 18 MB), which each GPU that loads libtc
+// size (kScratchBytes below, about 20 MB), which each GPU that loads libtc
 // keeps until the process exits.
 //
 // Limits: n_rows <= kMaxRows (262,144) and nnz <= kMaxNnz (2,097,152); larger
@@ -43,7 +43,8 @@ constexpr size_t kOffInOff = align256(kOffInCnt + sizeof(int32_t) * (kMaxRows + 
 constexpr size_t kOffInWork = align256(kOffInOff + sizeof(int32_t) * (kMaxRows + 2));
 constexpr size_t kOffOutWork = align256(kOffInWork + sizeof(unsigned long long) * (kMaxRows + 1));
 constexpr size_t kOffInList = align256(kOffOutWork + sizeof(unsigned long long) * (kMaxRows + 1));
-constexpr size_t kOffScan = align256(kOffInList + sizeof(int32_t) * kMaxNnz);
+constexpr size_t kOffMid = align256(kOffInList + sizeof(int32_t) * kMaxNnz);
+constexpr size_t kOffScan = align256(kOffMid + kMaxNnz);
 constexpr size_t kScratchBytes = align256(kOffScan + sizeof(int32_t) * kScanTmp);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -118,6 +119,7 @@ extern "C" int tc_count_noalloc_i32(const int32_t *d_row_ptr, const int32_t *d_c
     sc.in_work = (unsigned long long *)(base + kOffInWork);
     sc.out_work = (unsigned long long *)(base + kOffOutWork);
     sc.in_list = (int32_t *)(base + kOffInList);
+    sc.mid = (uint8_t *)(base + kOffMid);
     GraphDesc d;
     memset(&d, 0, sizeof d);
     d.rp = d_row_ptr;
