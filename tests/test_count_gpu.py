@@ -22,6 +22,8 @@ TUNINGS = [
     {"heavy_bitmap": 0, "warp_max_deg": 32, "light_max_work": 64},  # heavy work on shared hash tiles
     {"heavy_bitmap": 1, "warp_max_deg": 32, "light_max_work": 64},  # heavy work on the id bitmap kernel
     {"heavy_bitmap": 1},
+    {"hash_pairs": 1},  # bucketed-pair tables, light and heavy
+    {"hash_pairs": 1, "warp_max_deg": 32, "light_max_work": 64, "long_list": 5},
 ]
 
 
@@ -30,7 +32,7 @@ def tuned(ctx):
     old = ctx.get_tuning()
     yield ctx
     ctx.set_tuning(old["warp_max_deg"], old["light_max_work"], old["unit_work"], old["long_list"],
-                   old["probe_kicks"], old["heavy_bitmap"], 0)
+                   old["probe_kicks"], old["heavy_bitmap"], 0, old["hash_pairs"])
 
 
 @pytest.mark.parametrize("tuning", TUNINGS)

@@ -418,6 +418,7 @@ int tc_ctx_create(int device, tc_ctx **out) {
     c->tuning.probe_kicks = 32;
     c->tuning.heavy_bitmap = 0;  // an autotuner candidate: one 32-warp block per SM rarely pays off
     c->tuning.blocks_per_sm = 0;
+    c->tuning.hash_pairs = 0;
     int st = TC_OK;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) st = TC_E_CUDA;
     c->own_stream = true;
@@ -495,6 +496,7 @@ int tc_ctx_set_tuning(tc_ctx *c, const tc_tuning *in) {
     if (in->probe_kicks >= 0) t.probe_kicks = in->probe_kicks;
     if (in->heavy_bitmap >= 0) t.heavy_bitmap = in->heavy_bitmap;
     if (in->blocks_per_sm >= 0) t.blocks_per_sm = in->blocks_per_sm;
+    if (in->hash_pairs >= 0) t.hash_pairs = in->hash_pairs;
     Tuned r;
     TC_TRY(resolve_tuning(t, c->sm_count, &r));
     c->tuning = t;

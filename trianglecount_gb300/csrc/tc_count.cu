@@ -128,6 +128,52 @@ __device__ __forceinline__ uint32_t cuckoo_probe(const int *tab, int shift, int 
     return (uint32_t)((a == x) | (b == x));
 }
 
+// Bucketed pairs: slots 2b and 2b+1 form bucket b and are read together by
+// one 8-byte shared load; one hash picks a key's home bucket.  A key goes to
+// the first bucket from its home with a free slot, and every full bucket it
+// passes is flagged (bit 31 of the bucket's first slot, which is occupied), so
+// a lookup reads past a bucket only when that bucket is flagged.  At a load of
+// at most 1/4 (half a key per bucket on average) about 1.4% of the buckets
+// hold more than two home keys, so nearly every probe is one shared load --
+// against two for the cuckoo hash -- and random 8-byte loads conflict less per
+// key than two random 4-byte loads.  Keys are vertex ids <= 2^31 - 2, so a
+// flagged slot (key | 2^31, negative, not -1) never reads as empty or as a key.
+constexpr int kFlagBit = (int)0x80000000u;
+constexpr int kKeyBits = 0x7fffffff;
+
+__device__ __forceinline__ void pair_insert(int *tab, uint32_t bmask, int shift, int x) {
+    uint32_t b = hash_slot(x, shift + 1);
+    for (uint32_t it = 0; it <= bmask; ++it) {
+        if (atomicCAS(&tab[2 * b], kEmpty, x) == kEmpty) return;
+        if (atomicCAS(&tab[2 * b + 1], kEmpty, x) == kEmpty) return;
+        atomicOr(&tab[2 * b], kFlagBit);
+        b = (b + 1) & bmask;
+    }
+}
+
+__device__ __forceinline__ uint32_t pair_hit(int2 v, int x) { return (uint32_t)(((v.x & kKeyBits) == x) | (v.y == x)); }
+
+// The rest of a pair lookup after its home bucket v (read at b) missed and was
+// flagged.  The bound only guards against a corrupt table.
+__device__ __forceinline__ uint32_t pair_probe_rest(const int *tab, uint32_t bmask, uint32_t b, int x) {
+    const int2 *tv = reinterpret_cast<const int2 *>(tab);
+    for (uint32_t it = 0; it < bmask; ++it) {
+        b = (b + 1) & bmask;
+        const int2 v = tv[b];
+        if (pair_hit(v, x)) return 1u;
+        if (v.x >= kEmpty) return 0u;  // not flagged: the chain ends here
+    }
+    return 0u;
+}
+
+__device__ __forceinline__ uint32_t pair_probe(const int *tab, uint32_t bmask, int shift, int x) {
+    const uint32_t b = hash_slot(x, shift + 1);
+    const int2 v = reinterpret_cast<const int2 *>(tab)[b];
+    uint32_t h = pair_hit(v, x);
+    if (!h && v.x < kEmpty) h = pair_probe_rest(tab, bmask, b, x);
+    return h;
+}
+
 // Membership of x in a direct-address bitmap of vertex ids (bit x of word
 // x/32).  A negative x (a padding lane) reads word 0 and reports no hit, so
 // the load stays inside the bitmap.
@@ -136,9 +182,31 @@ __device__ __forceinline__ uint32_t bitmap_probe(const int *bm, int x) {
     return ((uint32_t)bm[(unsigned)y >> 5] >> (y & 31)) & (uint32_t)(x >= 0);
 }
 
-// Membership of x >= 0 in the table, by the table's mode.
-__device__ __forceinline__ uint32_t probe_any(const int *tab, uint32_t mask, int shift, int x, bool cuckoo) {
-    return cuckoo ? cuckoo_probe(tab, shift, x) : table_probe(tab, mask, shift, x);
+// Table modes, chosen per table (warp- or block-uniform).
+constexpr int kLinear = 0, kCuckoo = 1, kPairs = 2;
+
+// Membership of x >= 0 in the table, by the table's mode (kPairsOnly: the
+// kernel instance that builds pair tables only).
+template <bool kPairsOnly>
+__device__ __forceinline__ uint32_t probe_any(const int *tab, uint32_t mask, int shift, int x, int mode) {
+    if (kPairsOnly) return pair_probe(tab, mask >> 1, shift, x);
+    return mode == kCuckoo ? cuckoo_probe(tab, shift, x) : table_probe(tab, mask, shift, x);
+}
+
+// Fills an emptied table with the keys keys[i], i in [tid, n) step nthreads, in
+// the preferred mode; returns the mode the table ended in, or -1 when a cuckoo
+// insertion gave up (the caller then empties the table and inserts linearly).
+template <bool kPairsOnly>
+__device__ __forceinline__ int table_fill(int *tab, uint32_t mask, int shift, const int32_t *__restrict__ keys, int n,
+                                          int tid, int nthreads, int pref, int kicks, bool *ok) {
+    if (kPairsOnly) {
+        for (int i = tid; i < n; i += nthreads) pair_insert(tab, mask >> 1, shift, __ldg(keys + i));
+    } else if (pref == kCuckoo) {
+        for (int i = tid; i < n; i += nthreads) *ok &= cuckoo_insert(tab, shift, __ldg(keys + i), kicks);
+    } else {
+        for (int i = tid; i < n; i += nthreads) table_insert(tab, mask, shift, __ldg(keys + i));
+    }
+    return pref;
 }
 
 // Table geometry for n keys: slots = max(32, next_pow2(4 n)).
@@ -189,6 +257,7 @@ struct KParams {
     int tile;
     int long_list;
     int probe_kicks;  // 0: linear probing; > 0: cuckoo with this many kicks
+    int table_mode;   // preferred table mode: kPairs, kCuckoo (probe_kicks > 0) or kLinear
     int heavy_done;   // heavy units belong to heavy_bitmap_kernel: count_kernel skips phase A
 };
 
@@ -206,10 +275,10 @@ struct Task {
 // out-neighbours v of x, skipped unless d+(v) <= d+(x); the others are
 // in-neighbours u.  Returns this lane's hit count; with per_root set, hits are
 // also credited to their root (x for out-partners, u for in-partners).
-template <bool kPerRoot, bool kBitmap = false>
+template <bool kPerRoot, bool kBitmap = false, bool kPairsOnly = false>
 __device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
                                                    const Task &T, int j0, int j1, const int *tab, uint32_t mask,
-                                                   int shift, bool cuckoo, int long_list, int lane,
+                                                   int shift, int mode, int long_list, int lane,
                                                    unsigned long long *__restrict__ per_root) {
     uint32_t hits = 0;
     const int j = j0 + lane;
@@ -245,7 +314,23 @@ __device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ r
             if (kBitmap) {
 #pragma unroll
                 for (int i = 0; i < 4; ++i) h += (uint32_t)(x[i] >= 0) & bitmap_probe(tab, x[i]);
-            } else if (cuckoo) {
+            } else if (kPairsOnly) {
+                // the four home buckets first (independent loads), then the rare flagged chains
+                const uint32_t bmask = mask >> 1;
+                int2 v[4];
+                uint32_t b[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    b[i] = hash_slot(x[i], shift + 1);
+                    v[i] = reinterpret_cast<const int2 *>(tab)[b[i]];
+                }
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    uint32_t hi = pair_hit(v[i], x[i]);
+                    if (!hi && v[i].x < kEmpty && x[i] >= 0) hi = pair_probe_rest(tab, bmask, b[i], x[i]);
+                    h += (uint32_t)(x[i] >= 0) & hi;
+                }
+            } else if (mode == kCuckoo) {
 #pragma unroll
                 for (int i = 0; i < 4; ++i) h += (uint32_t)(x[i] >= 0) & cuckoo_probe(tab, shift, x[i]);
             } else {
@@ -285,7 +370,7 @@ __device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ r
         const int own = kPerRoot ? __shfl_sync(kFull, owner, seg) : 0;
         if (t < total) {
             const int y = __ldg(col + s_seg + (t - ex_seg));
-            const uint32_t h = kBitmap ? bitmap_probe(tab, y) : probe_any(tab, mask, shift, y, cuckoo);
+            const uint32_t h = kBitmap ? bitmap_probe(tab, y) : probe_any<kPairsOnly>(tab, mask, shift, y, mode);
             hits += h;
             if (kPerRoot && h) atomicAdd(per_root + own, 1ull);
         }
@@ -615,7 +700,7 @@ __global__ void __launch_bounds__(kBigThreads, 1) heavy_bitmap_kernel(KParams P,
             c = __shfl_sync(kFull, c, 0);
             const int jb = j0 + c * kHeavyChunk;
             if (jb >= j1) break;
-            hits += probe_partners<kPerRoot, true>(rp, col, T, jb, min(jb + kHeavyChunk, j1), bm, 0, 0, false,
+            hits += probe_partners<kPerRoot, true>(rp, col, T, jb, min(jb + kHeavyChunk, j1), bm, 0, 0, kLinear,
                                                    P.long_list, lane, G.per_root);
         }
         if (!kPerRoot) {
@@ -635,7 +720,7 @@ __global__ void __launch_bounds__(kBigThreads, 1) heavy_bitmap_kernel(KParams P,
     }
 }
 
-template <bool kPerRoot>
+template <bool kPerRoot, bool kPairsOnly>
 __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KParams P) {
     extern __shared__ int smem[];
     __shared__ unsigned s_unit;
@@ -660,7 +745,7 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
 
     // ---- phase A: heavy units, one block each ----
     int cached_entry = -1, cached_tile = -1;
-    bool cached_cuckoo = false;
+    int cached_mode = kLinear;
     for (; !P.heavy_done;) {
         if (warp == 0) {
             unsigned unit = 0;
@@ -717,17 +802,13 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
             table_clear(smem, mask, threadIdx.x, kThreads);
             __syncthreads();
             bool ok = true;
-            if (P.probe_kicks > 0)
-                for (int i = threadIdx.x; i < tl; i += kThreads)
-                    ok &= cuckoo_insert(smem, shift, __ldg(col + rs + t0 + i), P.probe_kicks);
-            cached_cuckoo = P.probe_kicks > 0 && !__syncthreads_or(!ok);
-            if (!cached_cuckoo) {  // linear probing (chosen, or after a cuckoo give-up)
-                if (P.probe_kicks > 0) {
-                    table_clear(smem, mask, threadIdx.x, kThreads);
-                    __syncthreads();
-                }
-                for (int i = threadIdx.x; i < tl; i += kThreads)
-                    table_insert(smem, mask, shift, __ldg(col + rs + t0 + i));
+            cached_mode = table_fill<kPairsOnly>(smem, mask, shift, col + rs + t0, tl, threadIdx.x, kThreads,
+                                                 P.table_mode, P.probe_kicks, &ok);
+            if (__syncthreads_or(!ok)) {  // a cuckoo give-up: linear probing instead
+                table_clear(smem, mask, threadIdx.x, kThreads);
+                __syncthreads();
+                cached_mode = table_fill<false>(smem, mask, shift, col + rs + t0, tl, threadIdx.x, kThreads, kLinear, 0,
+                                                &ok);
             }
             cached_entry = ei;
             cached_tile = ti;
@@ -742,8 +823,8 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
             c = __shfl_sync(kFull, c, 0);
             const int jb = j0 + c * kHeavyChunk;
             if (jb >= j1) break;
-            hits += probe_partners<kPerRoot>(rp, col, T, jb, min(jb + kHeavyChunk, j1), smem, mask, shift,
-                                             cached_cuckoo, P.long_list, lane, G.per_root);
+            hits += probe_partners<kPerRoot, false, kPairsOnly>(rp, col, T, jb, min(jb + kHeavyChunk, j1), smem, mask, shift,
+                                             cached_mode, P.long_list, lane, G.per_root);
         }
         if (!kPerRoot) {
             if (e.g != cur_g) flush(e.g);
@@ -792,21 +873,19 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
             table_clear(wtab, mask, lane, kWarp);
             __syncwarp();
             bool ok = true;
-            if (P.probe_kicks > 0)
-                for (int i = lane; i < T.dx; i += kWarp) ok &= cuckoo_insert(wtab, shift, __ldg(col + rrs + i), P.probe_kicks);
-            const bool cuckoo = P.probe_kicks > 0 && __all_sync(kFull, ok);
-            if (!cuckoo) {  // linear probing (chosen, or after a cuckoo give-up)
-                if (P.probe_kicks > 0) {
-                    __syncwarp();
-                    table_clear(wtab, mask, lane, kWarp);
-                    __syncwarp();
-                }
-                for (int i = lane; i < T.dx; i += kWarp) table_insert(wtab, mask, shift, __ldg(col + rrs + i));
+            int mode = table_fill<kPairsOnly>(wtab, mask, shift, col + rrs, T.dx, lane, kWarp, P.table_mode,
+                                              P.probe_kicks, &ok);
+            if (!__all_sync(kFull, ok)) {  // a cuckoo give-up: linear probing instead
+                __syncwarp();
+                table_clear(wtab, mask, lane, kWarp);
+                __syncwarp();
+                mode = table_fill<false>(wtab, mask, shift, col + rrs, T.dx, lane, kWarp, kLinear, 0, &ok);
             }
             __syncwarp();
             uint32_t hits = 0;
             for (int jb = 0; jb < n_part; jb += kWarp)
-                hits += probe_partners<kPerRoot>(rp, col, T, jb, min(jb + kWarp, n_part), wtab, mask, shift, cuckoo,
+                hits += probe_partners<kPerRoot, false, kPairsOnly>(rp, col, T, jb, min(jb + kWarp, n_part), wtab, mask,
+                                                                    shift, mode,
                                                  P.long_list, lane, G.per_root);
             __syncwarp();
             if (!kPerRoot) acc += hits;
@@ -839,6 +918,8 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     r.long_list = t.long_list >= 0 ? t.long_list : 32;
     r.probe_kicks = t.probe_kicks >= 0 ? t.probe_kicks : 32;
     r.heavy_bitmap = t.heavy_bitmap >= 0 ? t.heavy_bitmap : 0;
+    r.hash_pairs = t.hash_pairs >= 0 ? t.hash_pairs : 0;
+    if (r.hash_pairs > 1) return set_error(TC_E_INVALID, "hash_pairs must be 0 or 1, got %d", r.hash_pairs);
     r.sm_count = sm_count;
     {
         // the bitmap takes what one block may opt into, minus the kernel's static shared memory
@@ -857,10 +938,12 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     if (r.long_list > 4096) return set_error(TC_E_INVALID, "long_list must be <= 4096, got %d", r.long_list);
     r.threads = kThreads;
     r.smem = (size_t)block_slots * sizeof(int);
-    TC_CUDA(cudaFuncSetAttribute(count_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
-    TC_CUDA(cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
+    TC_CUDA(cudaFuncSetAttribute(count_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
+    TC_CUDA(cudaFuncSetAttribute(count_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
+    TC_CUDA(cudaFuncSetAttribute(count_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
+    TC_CUDA(cudaFuncSetAttribute(count_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
     int occ = 0;
-    TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, count_kernel<false>, kThreads, r.smem));
+    TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, count_kernel<false, false>, kThreads, r.smem));
     if (occ < 1) return set_error(TC_E_INVALID, "count kernel does not fit on an SM with %zu B shared memory", r.smem);
     const int bps = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, occ) : occ;
     r.blocks = sm_count * bps;
@@ -894,6 +977,7 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
     P.tile = tn.tile;
     P.long_list = tn.long_list;
     P.probe_kicks = tn.probe_kicks;
+    P.table_mode = tn.hash_pairs ? kPairs : tn.probe_kicks > 0 ? kCuckoo : kLinear;
     // heavy units on direct-address bitmaps when every graph's ids fit in shared memory
     const int64_t bitmap_words = (max_rows + 31) / 32;
     const bool bitmap = tn.heavy_bitmap && bitmap_words > 0 && bitmap_words * 4 <= (int64_t)tn.bitmap_bytes;
@@ -923,8 +1007,13 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
             TC_CUDA(cudaGetLastError());
             ++nl;
         }
-        if (per_root) count_kernel<true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
-        else count_kernel<false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        if (per_root) {
+            if (tn.hash_pairs) count_kernel<true, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+            else count_kernel<true, false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        } else {
+            if (tn.hash_pairs) count_kernel<false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+            else count_kernel<false, false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        }
         if (kev) TC_CUDA(cudaEventRecord(kev[1], s));
         TC_CUDA(cudaGetLastError());
         nl += 4 + (total_vertices > 4096 ? 3 : 1);
@@ -959,6 +1048,7 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
     P.tile = tn.tile;
     P.long_list = tn.long_list;
     P.probe_kicks = tn.probe_kicks;
+    P.table_mode = tn.hash_pairs ? kPairs : tn.probe_kicks > 0 ? kCuckoo : kLinear;
     P.heavy_done = 0;
     TC_CUDA(cudaMemsetAsync(work, 0, sizeof(CountWork), s));
     TC_CUDA(cudaMemsetAsync(results, 0, sizeof(unsigned long long), s));
@@ -974,7 +1064,7 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
         transpose_classify_kernel<<<aux_blocks, kThreads, 0, s>>>(P, sc.heavy);
         TC_CUDA(cudaGetLastError());
         micro_kernel<false><<<aux_blocks, kThreads, 0, s>>>(P);
-        count_kernel<false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        count_kernel<false, false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
         TC_CUDA(cudaGetLastError());
     }
     return TC_OK;

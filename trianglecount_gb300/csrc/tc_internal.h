@@ -113,6 +113,7 @@ struct Tuned {  // resolved tc_tuning with derived table geometry
     int long_list;
     int probe_kicks;     // 0: linear-probing hash; > 0: cuckoo hash with this kick bound
     int heavy_bitmap;    // 1: heavy units on direct-address bitmaps when the ids fit
+    int hash_pairs;      // 1: bucketed-pair hash tables (one 8-byte load per probe)
     int bitmap_bytes;    // shared memory the bitmap kernel may use (ids < 8 x this)
     int sm_count;
     int tile;            // block table entries per tile (a quarter of its slots)

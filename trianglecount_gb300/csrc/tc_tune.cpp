@@ -43,18 +43,19 @@ extern "C" int tc_autotune(tc_ctx *ctx, tc_graph *g, int max_trials, int reps, t
     float cur_ms = 0;
     TC_TRY(time_count(ctx, g, reps, &cur_ms));
     int trials = 1;
-    const std::vector<int32_t> grid[6] = {
+    const std::vector<int32_t> grid[7] = {
         {64, 128, 256, 512},
         {4096, 8192, 16384, 32768, 65536, 131072},
         {65536, 131072, 262144, 524288, 1048576},
         {8, 16, 32, 64},
         {0, 32},
         {0, 1},
+        {0, 1},
     };
     bool changed = true;
     while (changed && trials < max_trials) {
         changed = false;
-        for (int p = 0; p < 6 && trials < max_trials; ++p) {
+        for (int p = 0; p < 7 && trials < max_trials; ++p) {
             for (int32_t v : grid[p]) {
                 if (trials >= max_trials) break;
                 tc_tuning t = cur;
@@ -63,7 +64,8 @@ extern "C" int tc_autotune(tc_ctx *ctx, tc_graph *g, int max_trials, int reps, t
                                  : p == 2 ? &t.unit_work
                                  : p == 3 ? &t.long_list
                                  : p == 4 ? &t.probe_kicks
-                                          : &t.heavy_bitmap;
+                                 : p == 5 ? &t.heavy_bitmap
+                                          : &t.hash_pairs;
                 if (*field == v) continue;
                 *field = v;
                 TC_TRY(tc_ctx_set_tuning(ctx, &t));
