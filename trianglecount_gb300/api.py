@@ -254,6 +254,13 @@ class Context:
     def synchronize(self) -> None:
         N.call("tc_ctx_synchronize", self._h)
 
+    def last_count_kernel_ms(self) -> float:
+        """Device time of the last plain count's counting kernel (CUDA events
+        on the context's stream around it; waits for it)."""
+        ms = C.c_float()
+        N.call("tc_ctx_last_count_kernel_ms", self._h, C.byref(ms))
+        return ms.value
+
     def device_info(self) -> dict:
         sm, f, t = C.c_int(), C.c_size_t(), C.c_size_t()
         N.call("tc_ctx_device_info", self._h, C.byref(sm), C.byref(f), C.byref(t))

@@ -66,6 +66,7 @@ constexpr int kHeavyChunk = 4;  // partners per warp grab inside a heavy unit
 constexpr int kLaneRowDeg = 16; // auxiliary passes: rows with d+ <= this are walked one per lane
 constexpr int kMicroDeg = 8;    // micro tasks: d+(x) <= this (N+(x) held in registers) ...
 constexpr int kMicroWork = 512; // ... and at most this many probes (one lane runs the task)
+constexpr int kAuxGrab = 4;     // 32-row chunks an auxiliary-kernel warp takes per cursor grab
 #ifndef TC_COUNT_MIN_BLOCKS
 // Resident blocks per SM the count kernel's registers must allow: 6 caps it
 // at 40 registers (a few spilled bytes) for 48 warps per SM, ~10% faster on
@@ -259,6 +260,7 @@ struct KParams {
     int probe_kicks;  // 0: linear probing; > 0: cuckoo with this many kicks
     int table_mode;   // preferred table mode: kPairs, kCuckoo (probe_kicks > 0) or kLinear
     int heavy_done;   // heavy units belong to heavy_bitmap_kernel: count_kernel skips phase A
+    int aux_dynamic;  // auxiliary kernels walk chunks from cursors (batches) instead of grid-stride
 };
 
 // Where the partner p_j of task x lives and whose root it credits.
@@ -378,70 +380,94 @@ __device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ r
     return hits;
 }
 
+// Chunk walk of the auxiliary kernels.  One graph: a static grid-stride walk
+// over a grid larger than what is resident (the block scheduler balances it).
+// A batch (aux_dynamic): the resident grid grabs kAuxGrab chunks at a time
+// from a cursor, so the chunks in flight form one window moving through the
+// graphs in order (each graph's in-lists and hub lists stay hot in L2 while
+// it is walked, and heavy entries come out graph-ordered).  [c, c_end) is the
+// next range; c >= c_end means done.
+__device__ __forceinline__ void aux_next(const KParams &P, int k, int lane, bool first, int64_t &c, int64_t &c_end) {
+    if (P.aux_dynamic) {
+        unsigned cg = 0;
+        if (lane == 0) cg = atomicAdd(&P.work->aux_cursor[k], (unsigned)kAuxGrab);
+        cg = __shfl_sync(kFull, cg, 0);
+        c = (int64_t)cg;
+        c_end = min(c + kAuxGrab, P.total_chunks);
+    } else {
+        const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+        const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / kWarp;
+        c = first ? gwarp : c_end - 1 + nwarps;
+        c_end = min(c + 1, P.total_chunks);
+    }
+}
+
 // in_count: per root u of a 32-row chunk, per v in N+(u): middle-centric edges
 // (d+(u) < d+(v)) add one in-edge and d+(u) of work to v; the others add d+(v)
 // to u's root-centric work.
 __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
     const int lane = threadIdx.x & (kWarp - 1);
-    const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
-    const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / kWarp;
-    for (int64_t c = gwarp; c < P.total_chunks; c += nwarps) {
-        const int g = find_graph(P.gd, P.n_graphs, c);
-        const GraphDesc &G = P.gd[g];
-        const int32_t *__restrict__ rp = G.rp;
-        const int32_t *__restrict__ col = G.col;
-        const int64_t x0 = (c - G.chunk_base) * kWarp;
-        int rs = 0, d = 0;
-        if (x0 + lane < G.n_roots) {
-            rs = __ldg(rp + x0 + lane);
-            d = __ldg(rp + x0 + lane + 1) - rs;
-        }
-        // short rows: one per lane, four edges' loads in flight at a time
-        if (d >= 1 && d <= kLaneRowDeg) {
-            unsigned long long ow = 0;
-            for (int i0 = 0; i0 < d; i0 += 4) {
-                int v[4], dv[4];
+    int64_t c, c_end;
+    aux_next(P, 0, lane, true, c, c_end);
+    for (; c < c_end; aux_next(P, 0, lane, false, c, c_end)) {
+        for (; c < c_end; ++c) {
+            const int g = find_graph(P.gd, P.n_graphs, c);
+            const GraphDesc &G = P.gd[g];
+            const int32_t *__restrict__ rp = G.rp;
+            const int32_t *__restrict__ col = G.col;
+            const int64_t x0 = (c - G.chunk_base) * kWarp;
+            int rs = 0, d = 0;
+            if (x0 + lane < G.n_roots) {
+                rs = __ldg(rp + x0 + lane);
+                d = __ldg(rp + x0 + lane + 1) - rs;
+            }
+            // short rows: one per lane, four edges' loads in flight at a time
+            if (d >= 1 && d <= kLaneRowDeg) {
+                unsigned long long ow = 0;
+                for (int i0 = 0; i0 < d; i0 += 4) {
+                    int v[4], dv[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) v[q] = i0 + q < d ? __ldg(col + rs + i0 + q) : -1;
+                    for (int q = 0; q < 4; ++q) v[q] = i0 + q < d ? __ldg(col + rs + i0 + q) : -1;
 #pragma unroll
-                for (int q = 0; q < 4; ++q) dv[q] = v[q] >= 0 ? __ldg(rp + v[q] + 1) - __ldg(rp + v[q]) : 0;
+                    for (int q = 0; q < 4; ++q) dv[q] = v[q] >= 0 ? __ldg(rp + v[q] + 1) - __ldg(rp + v[q]) : 0;
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (v[q] < 0) continue;
-                    const bool m = d < dv[q];
-                    P.mid[G.ebase + rs + i0 + q] = (uint8_t)m;
-                    if (m) {
-                        atomicAdd(P.in_cnt + G.vbase + v[q], 1);
-                        atomicAdd(P.in_work + G.vbase + v[q], (unsigned long long)d);
-                    } else {
-                        ow += (unsigned long long)dv[q];
+                    for (int q = 0; q < 4; ++q) {
+                        if (v[q] < 0) continue;
+                        const bool m = d < dv[q];
+                        P.mid[G.ebase + rs + i0 + q] = (uint8_t)m;
+                        if (m) {
+                            atomicAdd(P.in_cnt + G.vbase + v[q], 1);
+                            atomicAdd(P.in_work + G.vbase + v[q], (unsigned long long)d);
+                        } else {
+                            ow += (unsigned long long)dv[q];
+                        }
                     }
                 }
+                P.out_work[G.vbase + x0 + lane] = ow;
             }
-            P.out_work[G.vbase + x0 + lane] = ow;
-        }
-        // long rows: the whole warp
-        unsigned todo = __ballot_sync(kFull, d > kLaneRowDeg);
-        while (todo) {
-            const int k = __ffs(todo) - 1;
-            todo &= todo - 1u;
-            const int rrs = __shfl_sync(kFull, rs, k);
-            const int rd = __shfl_sync(kFull, d, k);
-            unsigned long long ow = 0;
-            for (int i = lane; i < rd; i += kWarp) {
-                const int v = __ldg(col + rrs + i);
-                const int dv = __ldg(rp + v + 1) - __ldg(rp + v);
-                const bool m = rd < dv;
-                P.mid[G.ebase + rrs + i] = (uint8_t)m;
-                if (m) {
-                    atomicAdd(P.in_cnt + G.vbase + v, 1);
-                    atomicAdd(P.in_work + G.vbase + v, (unsigned long long)rd);
-                } else {
-                    ow += (unsigned long long)dv;
+            // long rows: the whole warp
+            unsigned todo = __ballot_sync(kFull, d > kLaneRowDeg);
+            while (todo) {
+                const int k = __ffs(todo) - 1;
+                todo &= todo - 1u;
+                const int rrs = __shfl_sync(kFull, rs, k);
+                const int rd = __shfl_sync(kFull, d, k);
+                unsigned long long ow = 0;
+                for (int i = lane; i < rd; i += kWarp) {
+                    const int v = __ldg(col + rrs + i);
+                    const int dv = __ldg(rp + v + 1) - __ldg(rp + v);
+                    const bool m = rd < dv;
+                    P.mid[G.ebase + rrs + i] = (uint8_t)m;
+                    if (m) {
+                        atomicAdd(P.in_cnt + G.vbase + v, 1);
+                        atomicAdd(P.in_work + G.vbase + v, (unsigned long long)rd);
+                    } else {
+                        ow += (unsigned long long)dv;
+                    }
                 }
+                ow = warp_sum_u64(ow);
+                if (lane == 0) P.out_work[G.vbase + x0 + k] = ow;
             }
-            ow = warp_sum_u64(ow);
-            if (lane == 0) P.out_work[G.vbase + x0 + k] = ow;
         }
     }
 }
@@ -451,154 +477,192 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
 // (block units) or no work.
 __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P, HeavyEntry *heavy) {
     const int lane = threadIdx.x & (kWarp - 1);
-    const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
-    const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / kWarp;
-    for (int64_t c = gwarp; c < P.total_chunks; c += nwarps) {
-        const int g = find_graph(P.gd, P.n_graphs, c);
-        const GraphDesc &G = P.gd[g];
-        const int32_t *__restrict__ rp = G.rp;
-        const int32_t *__restrict__ col = G.col;
-        const int64_t x0 = (c - G.chunk_base) * kWarp;
-        const int64_t x = x0 + lane;
-        int rs = 0, d = 0, nin = 0;
-        unsigned long long w = 0;
-        if (x < G.n_rows) {
-            rs = __ldg(rp + x);
-            d = __ldg(rp + x + 1) - rs;
-            nin = P.in_off[G.vbase + x + 1] - P.in_off[G.vbase + x];
-            w = P.out_work[G.vbase + x] + P.in_work[G.vbase + x];
-        }
-        // scatter the middle-centric out-edges of the chunk's roots (marked by
-        // in_count): short rows one per lane ...
-        if (d >= 1 && d <= kLaneRowDeg && x < G.n_roots) {
-            for (int i = 0; i < d; ++i) {
-                if (!P.mid[G.ebase + rs + i]) continue;
-                const int v = __ldg(col + rs + i);
-                const int pos = atomicSub(P.in_cnt + G.vbase + v, 1) - 1;
-                P.in_list[P.in_off[G.vbase + v] + pos] = (int32_t)x;
+    int64_t c, c_end;
+    aux_next(P, 1, lane, true, c, c_end);
+    for (; c < c_end; aux_next(P, 1, lane, false, c, c_end)) {
+        for (; c < c_end; ++c) {
+            const int g = find_graph(P.gd, P.n_graphs, c);
+            const GraphDesc &G = P.gd[g];
+            const int32_t *__restrict__ rp = G.rp;
+            const int32_t *__restrict__ col = G.col;
+            const int64_t x0 = (c - G.chunk_base) * kWarp;
+            const int64_t x = x0 + lane;
+            int rs = 0, d = 0, nin = 0;
+            unsigned long long w = 0;
+            if (x < G.n_rows) {
+                rs = __ldg(rp + x);
+                d = __ldg(rp + x + 1) - rs;
+                nin = P.in_off[G.vbase + x + 1] - P.in_off[G.vbase + x];
+                w = P.out_work[G.vbase + x] + P.in_work[G.vbase + x];
             }
-        }
-        // ... long rows by the whole warp
-        unsigned todo = __ballot_sync(kFull, d > kLaneRowDeg && x < G.n_roots);
-        while (todo) {
-            const int k = __ffs(todo) - 1;
-            todo &= todo - 1u;
-            const int rrs = __shfl_sync(kFull, rs, k);
-            const int rd = __shfl_sync(kFull, d, k);
-            for (int i = lane; i < rd; i += kWarp) {
-                if (!P.mid[G.ebase + rrs + i]) continue;
-                const int v = __ldg(col + rrs + i);
-                const int pos = atomicSub(P.in_cnt + G.vbase + v, 1) - 1;
-                P.in_list[P.in_off[G.vbase + v] + pos] = (int32_t)(x0 + k);
+            // scatter the middle-centric out-edges of the chunk's roots (marked by
+            // in_count): short rows one per lane ...
+            if (d >= 1 && d <= kLaneRowDeg && x < G.n_roots) {
+                for (int i = 0; i < d; ++i) {
+                    if (!P.mid[G.ebase + rs + i]) continue;
+                    const int v = __ldg(col + rs + i);
+                    const int pos = atomicSub(P.in_cnt + G.vbase + v, 1) - 1;
+                    P.in_list[P.in_off[G.vbase + v] + pos] = (int32_t)x;
+                }
             }
-        }
-        // classify
-        const bool has = w > 0 && d >= 1;
-        const bool micro = has && d <= kMicroDeg && w <= (unsigned long long)kMicroWork;
-        const bool light = has && !micro && d <= P.warp_max && w <= (unsigned long long)P.light_max_work;
-        const bool hv = has && !micro && !light;
-        const uint32_t mm = __ballot_sync(kFull, micro);
-        const uint32_t lm = __ballot_sync(kFull, light);
-        if (lane == 0) {
-            P.light_mask[c] = lm;
-            P.micro_mask[c] = mm;
-        }
-        unsigned hm = __ballot_sync(kFull, hv);
-        while (hm) {
-            const int k = __ffs(hm) - 1;
-            hm &= hm - 1u;
-            if (lane == k) {
-                const int n_part = (x < G.n_roots ? d : 0) + nin;
-                const int max_slices = max(1, (n_part + kHeavyChunk - 1) / kHeavyChunk);
-                int ns = (int)min((w + (unsigned long long)P.unit_work - 1) / (unsigned long long)P.unit_work,
-                                  (unsigned long long)max_slices);
-                ns = max(ns, 1);
-                const unsigned units = (unsigned)((d + P.tile - 1) / P.tile) * (unsigned)ns;
-                const unsigned long long base = atomicAdd(&P.work->heavy_packed, (1ull << 32) | units);
-                const unsigned long long idx = base >> 32;
-                if ((int64_t)idx < P.heavy_cap) {
-                    HeavyEntry e;
-                    e.g = g;
-                    e.u = (int32_t)x;
-                    e.unit_base = (int32_t)(unsigned)base;
-                    e.n_slices = ns;
-                    heavy[idx] = e;
-                } else {
-                    atomicExch(&P.work->error, 1);
+            // ... long rows by the whole warp
+            unsigned todo = __ballot_sync(kFull, d > kLaneRowDeg && x < G.n_roots);
+            while (todo) {
+                const int k = __ffs(todo) - 1;
+                todo &= todo - 1u;
+                const int rrs = __shfl_sync(kFull, rs, k);
+                const int rd = __shfl_sync(kFull, d, k);
+                for (int i = lane; i < rd; i += kWarp) {
+                    if (!P.mid[G.ebase + rrs + i]) continue;
+                    const int v = __ldg(col + rrs + i);
+                    const int pos = atomicSub(P.in_cnt + G.vbase + v, 1) - 1;
+                    P.in_list[P.in_off[G.vbase + v] + pos] = (int32_t)(x0 + k);
+                }
+            }
+            // classify
+            const bool has = w > 0 && d >= 1;
+            const bool micro = has && d <= kMicroDeg && w <= (unsigned long long)kMicroWork;
+            const bool light = has && !micro && d <= P.warp_max && w <= (unsigned long long)P.light_max_work;
+            const bool hv = has && !micro && !light;
+            const uint32_t mm = __ballot_sync(kFull, micro);
+            const uint32_t lm = __ballot_sync(kFull, light);
+            if (lane == 0) {
+                P.light_mask[c] = lm;
+                P.micro_mask[c] = mm;
+            }
+            unsigned hm = __ballot_sync(kFull, hv);
+            while (hm) {
+                const int k = __ffs(hm) - 1;
+                hm &= hm - 1u;
+                if (lane == k) {
+                    const int n_part = (x < G.n_roots ? d : 0) + nin;
+                    const int max_slices = max(1, (n_part + kHeavyChunk - 1) / kHeavyChunk);
+                    int ns = (int)min((w + (unsigned long long)P.unit_work - 1) / (unsigned long long)P.unit_work,
+                                      (unsigned long long)max_slices);
+                    ns = max(ns, 1);
+                    const unsigned units = (unsigned)((d + P.tile - 1) / P.tile) * (unsigned)ns;
+                    const unsigned long long base = atomicAdd(&P.work->heavy_packed, (1ull << 32) | units);
+                    const unsigned long long idx = base >> 32;
+                    if ((int64_t)idx < P.heavy_cap) {
+                        HeavyEntry e;
+                        e.g = g;
+                        e.u = (int32_t)x;
+                        e.unit_base = (int32_t)(unsigned)base;
+                        e.n_slices = ns;
+                        heavy[idx] = e;
+                    } else {
+                        atomicExch(&P.work->error, 1);
+                    }
                 }
             }
         }
     }
 }
 
+// A micro task compares lists of at most D ids (each loaded in one burst, two
+// lists in flight) with its d <= D register ids r; compares stop at the real
+// lengths (both sets are duplicate-free).
+template <int D>
+__device__ __forceinline__ void micro_load(const int32_t *__restrict__ lst, int len, int (&y)[D]) {
+#pragma unroll
+    for (int t = 0; t < D; ++t) y[t] = t < len ? __ldg(lst + t) : -2;
+}
+
+template <int D>
+__device__ __forceinline__ uint32_t micro_hits(const int (&y)[D], int len, const int (&r)[D], int d) {
+    uint32_t h = 0;
+#pragma unroll
+    for (int t = 0; t < D; ++t) {
+        if (t >= len) break;
+#pragma unroll
+        for (int q = 0; q < D; ++q) {
+            if (q >= d) break;
+            h += (uint32_t)(r[q] == y[t]);
+        }
+    }
+    return h;
+}
+
+// One micro task x (d+(x) = d <= D) on one lane; returns its hits (credited
+// per root when per_root is set).
+template <bool kPerRoot, int D>
+__device__ __forceinline__ uint32_t micro_task(const KParams &P, const GraphDesc &G, int x, int rs, int d) {
+    const int32_t *__restrict__ rp = G.rp;
+    const int32_t *__restrict__ col = G.col;
+    int r[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) r[i] = i < d ? __ldg(col + rs + i) : -1;
+    uint32_t own = 0;  // hits credited to x (root-centric partners)
+    if (x < G.n_roots) {
+        // every out-partner's row bounds at once, then each short list in one burst
+        int ps[D], pe[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+            ps[i] = r[i] >= 0 ? __ldg(rp + r[i]) : 0;
+            pe[i] = r[i] >= 0 ? __ldg(rp + r[i] + 1) : 0;
+        }
+#pragma unroll
+        for (int i = 0; i < D; i += 2) {
+            if (i >= d) break;
+            // a list longer than d is middle-centric: done from p's side
+            const int la = pe[i] - ps[i] <= d ? pe[i] - ps[i] : 0;
+            const int lb = pe[i + 1] - ps[i + 1] <= d ? pe[i + 1] - ps[i + 1] : 0;
+            int ya[D], yb[D];
+            micro_load<D>(col + ps[i], la, ya);
+            micro_load<D>(col + ps[i + 1], lb, yb);
+            own += micro_hits<D>(ya, la, r, d) + micro_hits<D>(yb, lb, r, d);
+        }
+    }
+    uint32_t in_hits = 0;
+    const int i0 = P.in_off[G.vbase + x], i1 = P.in_off[G.vbase + x + 1];
+    for (int k = i0; k < i1; k += 2) {  // in-partners (d+(u) < d+(x)), two at a time
+        const int pa = P.in_list[k];
+        const int pb = k + 1 < i1 ? P.in_list[k + 1] : -1;
+        const int sa = __ldg(rp + pa), la = __ldg(rp + pa + 1) - sa;
+        const int sb = pb >= 0 ? __ldg(rp + pb) : 0, lb = pb >= 0 ? __ldg(rp + pb + 1) - sb : 0;
+        int ya[D], yb[D];
+        micro_load<D>(col + sa, la, ya);
+        micro_load<D>(col + sb, lb, yb);
+        const uint32_t ha = micro_hits<D>(ya, la, r, d), hb = micro_hits<D>(yb, lb, r, d);
+        in_hits += ha + hb;
+        if (kPerRoot && ha) atomicAdd(G.per_root + pa, (unsigned long long)ha);
+        if (kPerRoot && hb) atomicAdd(G.per_root + pb, (unsigned long long)hb);
+    }
+    if (kPerRoot && own) atomicAdd(G.per_root + x, (unsigned long long)own);
+    return own + in_hits;
+}
+
 // micro tasks: one lane runs a whole task x (d+(x) <= kMicroDeg, work <=
 // kMicroWork) with N+(x) in registers; every streamed partner list is then at
-// most kMicroDeg long (the cheaper side), and membership is kMicroDeg
-// predicated compares -- no hash table, no shared memory.
+// most kMicroDeg long (the cheaper side), and membership is predicated
+// compares -- no hash table, no shared memory.  Tasks with d+(x) <= 4 (most
+// of a road network's) take a 4-wide path: a quarter of the compares.
 template <bool kPerRoot>
 __global__ void __launch_bounds__(kThreads) micro_kernel(KParams P) {
     const int lane = threadIdx.x & (kWarp - 1);
-    const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
-    const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / kWarp;
     unsigned long long acc = 0;
     int cur_g = -1;
-    for (int64_t c = gwarp; c < P.total_chunks; c += nwarps) {
-        const uint32_t mm = P.micro_mask[c];
-        if (!mm) continue;
-        const int g = find_graph(P.gd, P.n_graphs, c);
-        const GraphDesc &G = P.gd[g];
-        if (!kPerRoot && g != cur_g) {
-            const unsigned long long s = warp_sum_u64(acc);
-            if (lane == 0 && cur_g >= 0 && s) atomicAdd(P.results + cur_g, s);
-            acc = 0;
-            cur_g = g;
-        }
-        if (!((mm >> lane) & 1u)) continue;
-        const int32_t *__restrict__ rp = G.rp;
-        const int32_t *__restrict__ col = G.col;
-        const int x = (int)((c - G.chunk_base) * kWarp + lane);
-        const int rs = __ldg(rp + x);
-        const int d = __ldg(rp + x + 1) - rs;
-        int r[kMicroDeg];
-#pragma unroll
-        for (int i = 0; i < kMicroDeg; ++i) r[i] = i < d ? __ldg(col + rs + i) : -1;
-        uint32_t own = 0;  // hits credited to x (root-centric partners)
-        if (x < G.n_roots) {
-#pragma unroll
-            for (int i = 0; i < kMicroDeg; ++i) {
-                if (i >= d) break;
-                const int p = r[i];
-                const int s2 = __ldg(rp + p);
-                const int len = __ldg(rp + p + 1) - s2;
-                if (len > d) continue;  // middle-centric: done from p's side
-                for (int t = 0; t < len; ++t) {
-                    const int y = __ldg(col + s2 + t);
-                    uint32_t hit = 0;
-#pragma unroll
-                    for (int q = 0; q < kMicroDeg; ++q) hit |= (uint32_t)(r[q] == y);
-                    own += hit;
-                }
+    int64_t c, c_end;
+    aux_next(P, 2, lane, true, c, c_end);
+    for (; c < c_end; aux_next(P, 2, lane, false, c, c_end)) {
+        for (; c < c_end; ++c) {
+            const uint32_t mm = P.micro_mask[c];
+            if (!mm) continue;
+            const int g = find_graph(P.gd, P.n_graphs, c);
+            const GraphDesc &G = P.gd[g];
+            if (!kPerRoot && g != cur_g) {
+                const unsigned long long s = warp_sum_u64(acc);
+                if (lane == 0 && cur_g >= 0 && s) atomicAdd(P.results + cur_g, s);
+                acc = 0;
+                cur_g = g;
             }
-        }
-        uint32_t in_hits = 0;
-        const int i0 = P.in_off[G.vbase + x], i1 = P.in_off[G.vbase + x + 1];
-        for (int k = i0; k < i1; ++k) {
-            const int p = P.in_list[k];
-            const int s2 = __ldg(rp + p);
-            const int len = __ldg(rp + p + 1) - s2;
-            uint32_t hp = 0;
-            for (int t = 0; t < len; ++t) {
-                const int y = __ldg(col + s2 + t);
-#pragma unroll
-                for (int q = 0; q < kMicroDeg; ++q) hp += (uint32_t)(r[q] == y);
-            }
-            in_hits += hp;
-            if (kPerRoot && hp) atomicAdd(G.per_root + p, (unsigned long long)hp);
-        }
-        if (kPerRoot) {
-            if (own) atomicAdd(G.per_root + x, (unsigned long long)own);
-        } else {
-            acc += own + in_hits;
+            if (!((mm >> lane) & 1u)) continue;
+            const int x = (int)((c - G.chunk_base) * kWarp + lane);
+            const int rs = __ldg(G.rp + x);
+            const int d = __ldg(G.rp + x + 1) - rs;
+            const uint32_t h = d <= 4 ? micro_task<kPerRoot, 4>(P, G, x, rs, d)
+                                      : micro_task<kPerRoot, kMicroDeg>(P, G, x, rs, d);
+            if (!kPerRoot) acc += h;
         }
     }
     if (!kPerRoot) {
@@ -947,6 +1011,20 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     if (occ < 1) return set_error(TC_E_INVALID, "count kernel does not fit on an SM with %zu B shared memory", r.smem);
     const int bps = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, occ) : occ;
     r.blocks = sm_count * bps;
+    // The auxiliary kernels walk the 32-row chunks grid-stride.  With no more
+    // blocks than fit on the GPU at once, the chunks in flight form one moving
+    // window, so a batch touches its graphs (and their in-lists) one after the
+    // other instead of all at once, and heavy entries come out graph-ordered.
+    int aux_occ = 0, o = 0;
+    TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, in_count_kernel, kThreads, 0));
+    aux_occ = o;
+    TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, transpose_classify_kernel, kThreads, 0));
+    aux_occ = std::min(aux_occ, o);
+    TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, micro_kernel<false>, kThreads, 0));
+    aux_occ = std::min(aux_occ, o);
+    TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, micro_kernel<true>, kThreads, 0));
+    aux_occ = std::min(aux_occ, o);
+    r.aux_blocks = sm_count * std::max(1, aux_occ);
     *out = r;
     return TC_OK;
 }
@@ -991,7 +1069,9 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
         TC_CUDA(cudaMemsetAsync(sc.in_work, 0, sizeof(unsigned long long) * (size_t)total_vertices, s));
         TC_CUDA(cudaMemsetAsync(sc.out_work, 0, sizeof(unsigned long long) * (size_t)total_vertices, s));
         const int64_t want = (total_chunks + kWarpsPerBlock - 1) / kWarpsPerBlock;
-        const int aux_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)tn.blocks * 4));
+        P.aux_dynamic = n_graphs > 1 ? 1 : 0;
+        const int64_t cap = P.aux_dynamic ? (int64_t)tn.aux_blocks : (int64_t)tn.blocks * 4;
+        const int aux_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, cap));
         in_count_kernel<<<aux_blocks, kThreads, 0, s>>>(P);
         TC_CUDA(cudaGetLastError());
         TC_TRY(scan_exclusive_i32(sc.in_cnt, sc.in_off, total_vertices, s));
@@ -1057,6 +1137,7 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
         TC_CUDA(cudaMemsetAsync(sc.in_work, 0, sizeof(unsigned long long) * (size_t)total_vertices, s));
         TC_CUDA(cudaMemsetAsync(sc.out_work, 0, sizeof(unsigned long long) * (size_t)total_vertices, s));
         const int64_t want = (total_chunks + kWarpsPerBlock - 1) / kWarpsPerBlock;
+        P.aux_dynamic = 0;
         const int aux_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)tn.blocks * 4));
         in_count_kernel<<<aux_blocks, kThreads, 0, s>>>(P);
         TC_CUDA(cudaGetLastError());

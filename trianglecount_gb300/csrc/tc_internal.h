@@ -101,8 +101,8 @@ struct CountWork {
     unsigned long long heavy_packed; // (entries << 32) | units, from the classifier
     unsigned int heavy_cursor;
     unsigned int small_cursor;
+    unsigned int aux_cursor[3];      // chunk cursors of in_count, transpose/classify, micro
     int error;
-    int pad;
 };
 
 struct Tuned {  // resolved tc_tuning with derived table geometry
@@ -120,6 +120,7 @@ struct Tuned {  // resolved tc_tuning with derived table geometry
     int log_block_slots;
     int threads;         // per block
     int blocks;          // persistent grid
+    int aux_blocks;      // resident grid of the per-chunk auxiliary kernels
     size_t smem;         // dynamic shared memory bytes
 };
 
