@@ -100,9 +100,13 @@ TC_API int tc_ctx_device_info(tc_ctx *ctx, int *sm_count, size_t *free_bytes, si
  * vertex ids fit in one block's shared memory (about 1.85 M rows).
  * hash_pairs = 1 selects bucketed-pair tables instead (two slots per 8-byte
  * bucket, one hash, overflow flagged into the next bucket: nearly always one
- * shared load per lookup; never gives up).  In
+ * shared load per lookup; never gives up).  flat_max_deg (default 8): a
+ * graph none of whose rows is longer (known for uploaded and device-built
+ * graphs, not for wrapped ones) is counted by one kernel, one lane per root
+ * with N+(u) and each N+(v) in registers -- no transpose, no hash tables
+ * (road networks and other bounded-degree graphs).  In
  * tc_ctx_set_tuning, fields <= 0 (long_list, probe_kicks, heavy_bitmap,
- * blocks_per_sm, hash_pairs: < 0) keep the current value. */
+ * blocks_per_sm, hash_pairs, flat_max_deg: < 0) keep the current value. */
 typedef struct tc_tuning {
     int32_t warp_max_deg;   /* 32..512, power of two */
     int32_t light_max_work; /* wedge probes a light task may have */
@@ -112,6 +116,7 @@ typedef struct tc_tuning {
     int32_t heavy_bitmap;   /* 0 or 1 */
     int32_t blocks_per_sm;  /* persistent grid = SMs * this (0: occupancy) */
     int32_t hash_pairs;     /* 0 or 1: bucketed-pair hash tables instead of cuckoo / linear */
+    int32_t flat_max_deg;   /* 0, 4 or 8: a graph with no row longer than this counts in one kernel */
 } tc_tuning;
 TC_API int tc_ctx_get_tuning(tc_ctx *ctx, tc_tuning *out);
 TC_API int tc_ctx_set_tuning(tc_ctx *ctx, const tc_tuning *in);

@@ -23,6 +23,7 @@ TUNINGS = [
     {"heavy_bitmap": 1, "warp_max_deg": 32, "light_max_work": 64},  # heavy work on the id bitmap kernel
     {"heavy_bitmap": 1},
     {"hash_pairs": 1},  # bucketed-pair tables, light and heavy
+    {"flat_max_deg": 0},  # bounded-degree graphs through the full chain too
     {"hash_pairs": 1, "warp_max_deg": 32, "light_max_work": 64, "long_list": 5},
 ]
 
@@ -32,7 +33,7 @@ def tuned(ctx):
     old = ctx.get_tuning()
     yield ctx
     ctx.set_tuning(old["warp_max_deg"], old["light_max_work"], old["unit_work"], old["long_list"],
-                   old["probe_kicks"], old["heavy_bitmap"], 0, old["hash_pairs"])
+                   old["probe_kicks"], old["heavy_bitmap"], 0, old["hash_pairs"], old["flat_max_deg"])
 
 
 @pytest.mark.parametrize("tuning", TUNINGS)
@@ -75,7 +76,7 @@ def test_graph_families_match_oracle(ctx, maker, tie):
     g = ctx.upload(orp, ocl)
     got, st = ctx.count(g, stats=True)
     assert got == want
-    assert st["launches"] >= 4 and st["count_ms"] > 0
+    assert st["launches"] >= 1 and st["count_ms"] > 0
 
 
 def test_rmat_golden_counts_on_device(ctx, golden_dir):
@@ -148,3 +149,54 @@ def test_context_outlives_its_graphs():
     assert g.count() == want
     b.free()
     g.free()
+
+
+def _bounded_degree_cases():
+    """Graphs whose oriented rows are all at most 8 long (the flat count)."""
+    yield "road300", gen.road(300)
+    yield "road_tall", gen.road(64, height=900)
+    s, d, _ = families.complete(5)  # out-degrees 4..0: 4-wide variant
+    yield "K5", (s, d)
+    s, d, _ = families.complete(9)  # out-degrees 8..0: 8-wide variant
+    yield "K9", (s, d)
+    yield "er_sparse", gen.er(20000, 2.5, seed=21)
+    yield "er_deg6", gen.er(3000, 6.0, seed=5)  # out-degrees up to 7: 8-wide variant
+    yield "road_full", gen.road()  # 2.1 M vertices; out-degree 5 under the id tie
+
+
+@pytest.mark.parametrize("tie", ["reference", "id_asc"])
+def test_flat_count_matches_chain_and_oracle(tuned, tie):
+    for name, (src, dst) in _bounded_degree_cases():
+        orp, ocl, want = oracle.pipeline(src, dst, tie=tie)
+        assert np.diff(orp).max() <= 8, name
+        _, want_pr = oracle.count(orp, ocl, per_root=True)
+        g = tuned.upload(orp, ocl)
+        tuned.set_tuning(flat_max_deg=8)
+        got, st = tuned.count(g, stats=True)
+        assert got == want and st["launches"] == 1, name
+        assert np.array_equal(tuned.count_per_root(g), want_pr), name
+        tuned.set_tuning(flat_max_deg=0)  # the same graph through the full chain
+        got, st = tuned.count(g, stats=True)
+        assert got == want and st["launches"] >= 4, name
+        assert np.array_equal(tuned.count_per_root(g), want_pr), name
+        tuned.set_tuning(flat_max_deg=8)
+
+
+def test_flat_count_roots_subset_and_device_built(tuned):
+    src, dst = gen.road(200)
+    orp, ocl, _ = oracle.pipeline(src, dst)
+    for nr in (0, 1, 777, len(orp) // 2, len(orp) - 1):
+        g = tuned.upload(orp, ocl, n_roots=nr)
+        assert tuned.count(g) == oracle.count(orp, ocl, n_roots=nr)
+    g = tuned.graph_from_edges(src, dst)  # oriented on the device: the row bound is known too
+    got, st = tuned.count(g, stats=True)
+    assert got == oracle.count(orp, ocl) and st["launches"] == 1
+
+
+def test_flat_count_not_used_above_the_bound(tuned):
+    src, dst, _ = families.complete(10)  # out-degree 9 somewhere
+    orp, ocl, want = oracle.pipeline(src, dst)
+    got, st = tuned.count(tuned.upload(orp, ocl), stats=True)
+    assert got == want and st["launches"] >= 4
+    with pytest.raises(tc.TCError):
+        tuned.set_tuning(flat_max_deg=9)

@@ -31,7 +31,8 @@ class TCError(RuntimeError):
 class Tuning(C.Structure):
     _fields_ = [("warp_max_deg", C.c_int32), ("light_max_work", C.c_int32), ("unit_work", C.c_int32),
                 ("long_list", C.c_int32), ("probe_kicks", C.c_int32), ("heavy_bitmap", C.c_int32),
-                ("blocks_per_sm", C.c_int32), ("hash_pairs", C.c_int32)]
+                ("blocks_per_sm", C.c_int32), ("hash_pairs", C.c_int32),
+                ("flat_max_deg", C.c_int32)]
 
 
 class CountStats(C.Structure):

@@ -273,9 +273,9 @@ class Context:
 
     def set_tuning(self, warp_max_deg: int = 0, light_max_work: int = 0, unit_work: int = 0, long_list: int = -1,
                    probe_kicks: int = -1, heavy_bitmap: int = -1, blocks_per_sm: int = -1,
-                   hash_pairs: int = -1) -> None:
+                   hash_pairs: int = -1, flat_max_deg: int = -1) -> None:
         t = N.Tuning(warp_max_deg, light_max_work, unit_work, long_list, probe_kicks, heavy_bitmap, blocks_per_sm,
-                     hash_pairs)
+                     hash_pairs, flat_max_deg)
         N.call("tc_ctx_set_tuning", self._h, C.byref(t))
 
     def autotune(self, g: "Graph", max_trials: int = 32, reps: int = 3) -> tuple[dict, float]:

@@ -20,10 +20,12 @@ constexpr int kVersion = 10000;  // 1.0.0
 struct ValidateErr {
     int code;     // 0 ok, 1 row_ptr, 2 id range, 3 order
     int first;    // smallest offending row / entry index
+    int max_deg;  // longest row
 };
 
 __global__ void mark_rows_kernel(const int32_t *rp, int64_t n_rows, int64_t nnz, uint8_t *start, ValidateErr *err) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int longest = 0;
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n_rows; u += stride) {
         const int64_t a = rp[u], b = rp[u + 1];
         const bool bad = a > b || a < 0 || b > nnz || (u == 0 && a != 0) || (u == n_rows - 1 && b != nnz);
@@ -32,8 +34,21 @@ __global__ void mark_rows_kernel(const int32_t *rp, int64_t n_rows, int64_t nnz,
             atomicMin(&err->first, (int)u);
         } else if (a < b) {
             start[a] = 1;
+            longest = max(longest, (int)(b - a));
         }
     }
+    longest = __reduce_max_sync(0xffffffffu, longest);
+    if ((threadIdx.x & 31) == 0 && longest) atomicMax(&err->max_deg, longest);
+}
+
+// Longest row of a CSR (the out-degree bound that selects the flat count).
+__global__ void max_row_kernel(const int32_t *rp, int64_t n_rows, int *out) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int longest = 0;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n_rows; u += stride)
+        longest = max(longest, rp[u + 1] - rp[u]);
+    longest = __reduce_max_sync(0xffffffffu, longest);
+    if ((threadIdx.x & 31) == 0 && longest) atomicMax(out, longest);
 }
 
 __global__ void check_cols_kernel(const int32_t *col, int64_t nnz, int64_t n_rows, const uint8_t *start,
@@ -65,14 +80,15 @@ int grid_for(int64_t n, int sm) {
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)sm * 32));
 }
 
-int validate_csr_impl(tc_ctx *ctx, const int32_t *rp, const int32_t *col, int64_t n_rows, int64_t nnz) {
+int validate_csr_impl(tc_ctx *ctx, const int32_t *rp, const int32_t *col, int64_t n_rows, int64_t nnz,
+                      int32_t *max_deg = nullptr) {
     cudaStream_t s = ctx->stream;
     DBuf<uint8_t> start;
     DBuf<ValidateErr> err;
     TC_TRY(start.alloc((size_t)nnz + 1, s));
     TC_TRY(err.alloc(1, s));
     TC_CUDA(cudaMemsetAsync(start.p, 0, (size_t)nnz + 1, s));
-    ValidateErr init{0, 0x7fffffff};
+    ValidateErr init{0, 0x7fffffff, 0};
     TC_CUDA(cudaMemcpyAsync(err.p, &init, sizeof(init), cudaMemcpyHostToDevice, s));
     if (n_rows > 0) {
         mark_rows_kernel<<<grid_for(n_rows, ctx->sm_count), 256, 0, s>>>(rp, n_rows, nnz, start.p, err.p);
@@ -90,7 +106,9 @@ int validate_csr_impl(tc_ctx *ctx, const int32_t *rp, const int32_t *col, int64_
     case 1: return set_error(TC_E_FORMAT, "row_ptr is not a valid offset array at row %d", h.first);
     case 2: return set_error(TC_E_FORMAT, "column id out of range [0, %lld) at entry %d", (long long)n_rows, h.first);
     case 3: return set_error(TC_E_FORMAT, "row not strictly ascending at entry %d", h.first);
-    default: return TC_OK;
+    default:
+        if (max_deg) *max_deg = h.max_deg;
+        return TC_OK;
     }
 }
 
@@ -107,6 +125,8 @@ int ensure_count_scratch(tc_graph *g) {
         TC_TRY(dalloc(&p, sizeof(CountWork) + sizeof(unsigned long long), ctx->stream));
         g->d_work = (CountWork *)p;
         g->d_result = (unsigned long long *)(g->d_work + 1);
+    }
+    if (!g->d_desc) {  // the flat count needs only the work words
         TC_TRY(dalloc((void **)&g->d_desc, sizeof(GraphDesc), ctx->stream));
         TC_TRY(scratch_alloc(&g->sc, g->n_rows + 1, (g->n_rows + 31) / 32, g->nnz,
                              std::min(g->n_rows, g->nnz) + 1, ctx->stream));
@@ -116,6 +136,18 @@ int ensure_count_scratch(tc_graph *g) {
 
 int enqueue_graph_count(tc_graph *g, unsigned long long *per_root, unsigned long long *results, int *launches) {
     tc_ctx *ctx = g->ctx;
+    if (g->max_deg >= 0 && g->max_deg <= ctx->tuned.flat_max_deg) {
+        // every list fits a lane's registers: one kernel, no transpose or hash tables
+        if (!g->d_work) {
+            void *p = nullptr;
+            TC_TRY(dalloc(&p, sizeof(CountWork) + sizeof(unsigned long long), ctx->stream));
+            g->d_work = (CountWork *)p;
+            g->d_result = (unsigned long long *)(g->d_work + 1);
+        }
+        ctx->kev_recorded = true;
+        return launch_flat(g->rp, g->col, g->n_roots, g->max_deg, g->d_work, results ? results : g->d_result,
+                           per_root, ctx->tuned, ctx->stream, launches, ctx->kev);
+    }
     TC_TRY(ensure_count_scratch(g));
     GraphDesc d;
     memset(&d, 0, sizeof d);
@@ -351,6 +383,28 @@ int graph_adopt_device(tc_ctx *ctx, int32_t *rp, int32_t *col, int64_t n_rows, i
     g->rp = rp;
     g->col = col;
     g->owns = true;
+    if (n_rows > 0) {  // the longest row, for the flat count
+        cudaStream_t s = ctx->stream;
+        DBuf<int> d;
+        int h = 0;
+        int st = d.alloc(1, s);
+        if (st == TC_OK && cudaMemsetAsync(d.p, 0, sizeof(int), s) != cudaSuccess) st = TC_E_CUDA;
+        if (st == TC_OK) {
+            max_row_kernel<<<grid_for(n_rows, ctx->sm_count), 256, 0, s>>>(rp, n_rows, d.p);
+            if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(&h, d.p, sizeof(int), cudaMemcpyDeviceToHost, s) !=
+                                                         cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess)
+                st = set_error(TC_E_CUDA, "row length scan failed");
+        }
+        if (st != TC_OK) {
+            g->owns = false;  // the caller still owns rp / col on failure
+            tc_graph_destroy(g);
+            return st;
+        }
+        g->max_deg = h;
+    } else {
+        g->max_deg = 0;
+    }
     *out = g;
     return TC_OK;
 }
@@ -419,6 +473,7 @@ int tc_ctx_create(int device, tc_ctx **out) {
     c->tuning.heavy_bitmap = 0;  // an autotuner candidate: one 32-warp block per SM rarely pays off
     c->tuning.blocks_per_sm = 0;
     c->tuning.hash_pairs = 0;
+    c->tuning.flat_max_deg = 8;
     int st = TC_OK;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) st = TC_E_CUDA;
     c->own_stream = true;
@@ -497,6 +552,7 @@ int tc_ctx_set_tuning(tc_ctx *c, const tc_tuning *in) {
     if (in->heavy_bitmap >= 0) t.heavy_bitmap = in->heavy_bitmap;
     if (in->blocks_per_sm >= 0) t.blocks_per_sm = in->blocks_per_sm;
     if (in->hash_pairs >= 0) t.hash_pairs = in->hash_pairs;
+    if (in->flat_max_deg >= 0) t.flat_max_deg = in->flat_max_deg;
     Tuned r;
     TC_TRY(resolve_tuning(t, c->sm_count, &r));
     c->tuning = t;
@@ -519,7 +575,7 @@ int tc_graph_upload_i32(tc_ctx *ctx, const int32_t *row_ptr, const int32_t *col,
     if (st == TC_OK && nnz > 0 &&
         cudaMemcpyAsync(g->col, col, sizeof(int32_t) * (size_t)nnz, cudaMemcpyHostToDevice, s) != cudaSuccess)
         st = set_error(TC_E_CUDA, "col upload failed");
-    if (st == TC_OK) st = validate_csr_impl(ctx, g->rp, g->col, n_rows, nnz);
+    if (st == TC_OK) st = validate_csr_impl(ctx, g->rp, g->col, n_rows, nnz, &g->max_deg);
     if (st != TC_OK) {
         tc_graph_destroy(g);
         return st;
@@ -561,7 +617,7 @@ int tc_graph_upload_u64(tc_ctx *ctx, const uint64_t *row_ptr, const uint64_t *co
                         cudaStreamSynchronize(s) != cudaSuccess))
         st = set_error(TC_E_CUDA, "u64 narrowing failed");
     if (st == TC_OK && h_ovf) st = set_error(TC_E_RANGE, "u64 CSR value does not fit int32");
-    if (st == TC_OK) st = validate_csr_impl(ctx, g->rp, g->col, n_rows, nnz);
+    if (st == TC_OK) st = validate_csr_impl(ctx, g->rp, g->col, n_rows, nnz, &g->max_deg);
     if (st != TC_OK) {
         tc_graph_destroy(g);
         return st;

@@ -671,6 +671,48 @@ __global__ void __launch_bounds__(kThreads) micro_kernel(KParams P) {
     }
 }
 
+// flat count: for graphs whose every row has at most D entries, one lane per
+// root u holds N+(u) in registers and compares every N+(v), v in N+(u),
+// against it -- the reference's per-edge intersection, with no transpose, no
+// classification and no hash tables.  Row bounds of all v are loaded at once
+// and two lists are in flight, as in the micro tasks.  The lanes wait on four
+// dependent loads per root, so residency is what hides it: the 4-wide count
+// fits 32 registers, a full 2048 threads per SM.
+template <bool kPerRoot, int D>
+__global__ void __launch_bounds__(kThreads, (D <= 4 && !kPerRoot) ? 8 : 1) flat_kernel(const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
+                                                        int64_t n_roots, unsigned long long *result,
+                                                        unsigned long long *per_root) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    unsigned long long acc = 0;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n_roots; u += stride) {
+        const int rs = __ldg(rp + u);
+        const int d = __ldg(rp + u + 1) - rs;
+        int r[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) r[i] = i < d ? __ldg(col + rs + i) : -1;
+        int ps[D], pe[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+            ps[i] = r[i] >= 0 ? __ldg(rp + r[i]) : 0;
+            pe[i] = r[i] >= 0 ? __ldg(rp + r[i] + 1) : 0;
+        }
+        uint32_t h = 0;
+#pragma unroll
+        for (int i = 0; i < D; i += 2) {
+            if (i >= d) break;
+            const int la = pe[i] - ps[i], lb = pe[i + 1] - ps[i + 1];
+            int ya[D], yb[D];
+            micro_load<D>(col + ps[i], la, ya);
+            micro_load<D>(col + ps[i + 1], lb, yb);
+            h += micro_hits<D>(ya, la, r, d) + micro_hits<D>(yb, lb, r, d);
+        }
+        if (kPerRoot) per_root[u] = h;
+        acc += h;
+    }
+    acc = warp_sum_u64(acc);
+    if ((threadIdx.x & (kWarp - 1)) == 0 && acc) atomicAdd(result, acc);
+}
+
 // Heavy units with a direct-address bitmap of N+(x) over all vertex ids in
 // shared memory (graphs of at most bitmap_words * 32 rows): one shared load per
 // probe instead of the two of the cuckoo hash, and no tiling of N+(x).  One
@@ -984,6 +1026,9 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     r.heavy_bitmap = t.heavy_bitmap >= 0 ? t.heavy_bitmap : 0;
     r.hash_pairs = t.hash_pairs >= 0 ? t.hash_pairs : 0;
     if (r.hash_pairs > 1) return set_error(TC_E_INVALID, "hash_pairs must be 0 or 1, got %d", r.hash_pairs);
+    r.flat_max_deg = t.flat_max_deg >= 0 ? t.flat_max_deg : 8;
+    if (r.flat_max_deg > kMicroDeg)
+        return set_error(TC_E_INVALID, "flat_max_deg must be in [0, %d], got %d", kMicroDeg, r.flat_max_deg);
     r.sm_count = sm_count;
     {
         // the bitmap takes what one block may opt into, minus the kernel's static shared memory
@@ -1099,6 +1144,30 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
         nl += 4 + (total_vertices > 4096 ? 3 : 1);
     }
     if (launches) *launches = nl;
+    return TC_OK;
+}
+
+int launch_flat(const int32_t *rp, const int32_t *col, int64_t n_roots, int max_deg, CountWork *work,
+                unsigned long long *result, unsigned long long *per_root, const Tuned &tn, cudaStream_t s,
+                int *launches, cudaEvent_t *kev) {
+    if (max_deg > kMicroDeg) return set_error(TC_E_INVALID, "flat count needs rows of at most %d entries", kMicroDeg);
+    TC_CUDA(cudaMemsetAsync(work, 0, sizeof(CountWork), s));
+    TC_CUDA(cudaMemsetAsync(result, 0, sizeof(unsigned long long), s));
+    if (kev) TC_CUDA(cudaEventRecord(kev[0], s));
+    if (n_roots > 0) {
+        const int64_t want = (n_roots + kThreads - 1) / kThreads;
+        const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)tn.blocks * 8));
+        if (max_deg <= 4) {
+            if (per_root) flat_kernel<true, 4><<<blocks, kThreads, 0, s>>>(rp, col, n_roots, result, per_root);
+            else flat_kernel<false, 4><<<blocks, kThreads, 0, s>>>(rp, col, n_roots, result, per_root);
+        } else {
+            if (per_root) flat_kernel<true, kMicroDeg><<<blocks, kThreads, 0, s>>>(rp, col, n_roots, result, per_root);
+            else flat_kernel<false, kMicroDeg><<<blocks, kThreads, 0, s>>>(rp, col, n_roots, result, per_root);
+        }
+        TC_CUDA(cudaGetLastError());
+    }
+    if (kev) TC_CUDA(cudaEventRecord(kev[1], s));
+    if (launches) *launches = n_roots > 0 ? 1 : 0;
     return TC_OK;
 }
 

@@ -114,6 +114,7 @@ struct Tuned {  // resolved tc_tuning with derived table geometry
     int probe_kicks;     // 0: linear-probing hash; > 0: cuckoo hash with this kick bound
     int heavy_bitmap;    // 1: heavy units on direct-address bitmaps when the ids fit
     int hash_pairs;      // 1: bucketed-pair hash tables (one 8-byte load per probe)
+    int flat_max_deg;    // graphs whose rows are all this short count with flat_kernel (0: never)
     int bitmap_bytes;    // shared memory the bitmap kernel may use (ids < 8 x this)
     int sm_count;
     int tile;            // block table entries per tile (a quarter of its slots)
@@ -138,6 +139,13 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
 // descriptors on stream s; total_vertices = sum (n_rows + 1).
 // max_rows = largest n_rows among the graphs.  kev (optional, two events) is
 // recorded around the counting kernels (heavy bitmap + persistent count).
+// One-kernel count of a graph whose rows are all at most max_deg <= 8 long
+// (one lane per root, lists in registers); fills the work words and result
+// like launch_count.
+int launch_flat(const int32_t *rp, const int32_t *col, int64_t n_roots, int max_deg, CountWork *work,
+                unsigned long long *result, unsigned long long *per_root, const Tuned &tn, cudaStream_t s,
+                int *launches, cudaEvent_t *kev);
+
 int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, int64_t total_vertices,
                  int64_t max_rows, const CountScratch &sc, CountWork *work, unsigned long long *results, bool per_root,
                  const Tuned &tn, cudaStream_t s, int *launches, cudaEvent_t *kev = nullptr);
@@ -195,6 +203,7 @@ struct tc_graph {
     int32_t *rp = nullptr;
     int32_t *col = nullptr;
     int64_t n_rows = 0, nnz = 0, n_roots = 0;
+    int32_t max_deg = -1;  // longest row, when known (uploads and device-built graphs)
     bool owns = true;
     // per-graph count scratch, sized on first use
     tc::GraphDesc *d_desc = nullptr;

@@ -77,6 +77,7 @@ int setup_device(int dev, DeviceSetup **out) {
         t.heavy_bitmap = 0;  // the allocation-free variant keeps the fixed heavy path
         t.blocks_per_sm = 0;
         t.hash_pairs = 0;
+        t.flat_max_deg = 0;  // the flat count is not used here
         TC_TRY(resolve_tuning(t, device_sm_count(dev), &d.tuned));
         d.scratch = (unsigned char *)p;
         d.ready = true;

@@ -43,7 +43,7 @@ extern "C" int tc_autotune(tc_ctx *ctx, tc_graph *g, int max_trials, int reps, t
     float cur_ms = 0;
     TC_TRY(time_count(ctx, g, reps, &cur_ms));
     int trials = 1;
-    const std::vector<int32_t> grid[7] = {
+    const std::vector<int32_t> grid[8] = {
         {64, 128, 256, 512},
         {4096, 8192, 16384, 32768, 65536, 131072},
         {65536, 131072, 262144, 524288, 1048576},
@@ -51,11 +51,12 @@ extern "C" int tc_autotune(tc_ctx *ctx, tc_graph *g, int max_trials, int reps, t
         {0, 32},
         {0, 1},
         {0, 1},
+        {0, 4, 8},
     };
     bool changed = true;
     while (changed && trials < max_trials) {
         changed = false;
-        for (int p = 0; p < 7 && trials < max_trials; ++p) {
+        for (int p = 0; p < 8 && trials < max_trials; ++p) {
             for (int32_t v : grid[p]) {
                 if (trials >= max_trials) break;
                 tc_tuning t = cur;
@@ -65,7 +66,8 @@ extern "C" int tc_autotune(tc_ctx *ctx, tc_graph *g, int max_trials, int reps, t
                                  : p == 3 ? &t.long_list
                                  : p == 4 ? &t.probe_kicks
                                  : p == 5 ? &t.heavy_bitmap
-                                          : &t.hash_pairs;
+                                 : p == 6 ? &t.hash_pairs
+                                          : &t.flat_max_deg;
                 if (*field == v) continue;
                 *field = v;
                 TC_TRY(tc_ctx_set_tuning(ctx, &t));
