@@ -67,6 +67,8 @@ constexpr int kLaneRowDeg = 16; // auxiliary passes: rows with d+ <= this are wa
 constexpr int kMicroDeg = 8;    // micro tasks: d+(x) <= this (N+(x) held in registers) ...
 constexpr int kMicroWork = 512; // ... and at most this many probes (one lane runs the task)
 constexpr int kAuxGrab = 4;     // 32-row chunks an auxiliary-kernel warp takes per cursor grab
+constexpr int kMinUnit = 8192;  // smallest heavy block unit (probes)
+constexpr int kMinLight = 1024; // smallest light-task bound (probes)
 #ifndef TC_COUNT_MIN_BLOCKS
 // Resident blocks per SM the count kernel's registers must allow: 6 caps it
 // at 40 registers (a few spilled bytes) for 48 warps per SM, ~10% faster on
@@ -261,6 +263,7 @@ struct KParams {
     int table_mode;   // preferred table mode: kPairs, kCuckoo (probe_kicks > 0) or kLinear
     int heavy_done;   // heavy units belong to heavy_bitmap_kernel: count_kernel skips phase A
     int aux_dynamic;  // auxiliary kernels walk chunks from cursors (batches) instead of grid-stride
+    int count_blocks; // persistent grid of count_kernel
 };
 
 // Where the partner p_j of task x lives and whose root it credits.
@@ -407,6 +410,7 @@ __device__ __forceinline__ void aux_next(const KParams &P, int k, int lane, bool
 // to u's root-centric work.
 __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
     const int lane = threadIdx.x & (kWarp - 1);
+    unsigned long long probes = 0;  // this lane's share of sum_{u->v} min(d+(u), d+(v))
     int64_t c, c_end;
     aux_next(P, 0, lane, true, c, c_end);
     for (; c < c_end; aux_next(P, 0, lane, false, c, c_end)) {
@@ -438,12 +442,14 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
                         if (m) {
                             atomicAdd(P.in_cnt + G.vbase + v[q], 1);
                             atomicAdd(P.in_work + G.vbase + v[q], (unsigned long long)d);
+                            probes += (unsigned long long)d;
                         } else {
                             ow += (unsigned long long)dv[q];
                         }
                     }
                 }
                 P.out_work[G.vbase + x0 + lane] = ow;
+                probes += ow;
             }
             // long rows: the whole warp
             unsigned todo = __ballot_sync(kFull, d > kLaneRowDeg);
@@ -461,15 +467,20 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
                     if (m) {
                         atomicAdd(P.in_cnt + G.vbase + v, 1);
                         atomicAdd(P.in_work + G.vbase + v, (unsigned long long)rd);
+                        probes += (unsigned long long)rd;
                     } else {
                         ow += (unsigned long long)dv;
                     }
                 }
+                probes += ow;
                 ow = warp_sum_u64(ow);
                 if (lane == 0) P.out_work[G.vbase + x0 + k] = ow;
             }
         }
     }
+    // every edge's probes (the cheaper side) once, for the classifier's unit size
+    probes = warp_sum_u64(probes);
+    if (lane == 0 && probes) atomicAdd(&P.work->total_work, probes);
 }
 
 // transpose + classify: scatter the chunk's middle-centric edges into the
@@ -477,6 +488,17 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
 // (block units) or no work.
 __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P, HeavyEntry *heavy) {
     const int lane = threadIdx.x & (kWarp - 1);
+    // Block-unit size: unit_work, or less on a small job so that every count
+    // block gets about four units; the light-task bound likewise, so that a
+    // warp's largest light task is at most a quarter of a fair share (one unit
+    // is one block's work, one light task one warp's: on a small graph, a
+    // large one would be the whole kernel's tail).
+    const unsigned long long total = P.work->total_work;
+    const unsigned long long unit =
+        min((unsigned long long)P.unit_work, max((unsigned long long)kMinUnit, total / (4ull * P.count_blocks)));
+    const unsigned long long light_max =
+        min((unsigned long long)P.light_max_work,
+            max((unsigned long long)kMinLight, total / (4ull * P.count_blocks * kWarpsPerBlock)));
     int64_t c, c_end;
     aux_next(P, 1, lane, true, c, c_end);
     for (; c < c_end; aux_next(P, 1, lane, false, c, c_end)) {
@@ -522,7 +544,7 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
             // classify
             const bool has = w > 0 && d >= 1;
             const bool micro = has && d <= kMicroDeg && w <= (unsigned long long)kMicroWork;
-            const bool light = has && !micro && d <= P.warp_max && w <= (unsigned long long)P.light_max_work;
+            const bool light = has && !micro && d <= P.warp_max && w <= light_max;
             const bool hv = has && !micro && !light;
             const uint32_t mm = __ballot_sync(kFull, micro);
             const uint32_t lm = __ballot_sync(kFull, light);
@@ -537,8 +559,7 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
                 if (lane == k) {
                     const int n_part = (x < G.n_roots ? d : 0) + nin;
                     const int max_slices = max(1, (n_part + kHeavyChunk - 1) / kHeavyChunk);
-                    int ns = (int)min((w + (unsigned long long)P.unit_work - 1) / (unsigned long long)P.unit_work,
-                                      (unsigned long long)max_slices);
+                    int ns = (int)min((w + unit - 1) / unit, (unsigned long long)max_slices);
                     ns = max(ns, 1);
                     const unsigned units = (unsigned)((d + P.tile - 1) / P.tile) * (unsigned)ns;
                     const unsigned long long base = atomicAdd(&P.work->heavy_packed, (1ull << 32) | units);
@@ -1101,6 +1122,7 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
     P.long_list = tn.long_list;
     P.probe_kicks = tn.probe_kicks;
     P.table_mode = tn.hash_pairs ? kPairs : tn.probe_kicks > 0 ? kCuckoo : kLinear;
+    P.count_blocks = tn.blocks;
     // heavy units on direct-address bitmaps when every graph's ids fit in shared memory
     const int64_t bitmap_words = (max_rows + 31) / 32;
     const bool bitmap = tn.heavy_bitmap && bitmap_words > 0 && bitmap_words * 4 <= (int64_t)tn.bitmap_bytes;
@@ -1198,6 +1220,7 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
     P.long_list = tn.long_list;
     P.probe_kicks = tn.probe_kicks;
     P.table_mode = tn.hash_pairs ? kPairs : tn.probe_kicks > 0 ? kCuckoo : kLinear;
+    P.count_blocks = tn.blocks;
     P.heavy_done = 0;
     TC_CUDA(cudaMemsetAsync(work, 0, sizeof(CountWork), s));
     TC_CUDA(cudaMemsetAsync(results, 0, sizeof(unsigned long long), s));

@@ -103,6 +103,7 @@ struct CountWork {
     unsigned int small_cursor;
     unsigned int aux_cursor[3];      // chunk cursors of in_count, transpose/classify, micro
     int error;
+    unsigned long long total_work;   // sum over oriented edges of the cheaper side's length
 };
 
 struct Tuned {  // resolved tc_tuning with derived table geometry
