@@ -1,7 +1,7 @@
 """Benchmark: exact triangle counting throughput (oriented edges/s) on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload rmat21|road|rmat16|rmat23]
+                    [--workload rmat21|road|rmat16|rmat18|rmat23|rmat23_parts|batch256|serve|refstudy]
 
 One step = one exact count of the workload graph (classify + persistent count
 kernel, or the one flat kernel for a graph with no row longer than 8; result
@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["rmat21", "road", "rmat16", "rmat18", "rmat23", "rmat23_parts", "batch256",
+                                           "refstudy",
                                            "serve"], default="rmat21")
     ap.add_argument("--rates", default="50,200,1000,4000", help="serve: Poisson arrival rates (requests/s)")
     ap.add_argument("--requests", type=int, default=400, help="serve: requests per rate")
@@ -403,6 +404,59 @@ def _timed(stream, flush, fn, steps, warmup):
     return sum(ms) / len(ms)
 
 
+def run_refstudy(args, world, rank, local, pg):
+    """The reference's design-space study re-run on this GPU: its Find_Triangle
+    variants built from their own sources (src/WithoutPartition/:
+    ShareKernelTCV62_update_v1.cu 128 threads, shareMemSize.cu 64 threads,
+    With_Atomic_op.cu 256 threads with one atomic per probe,
+    Without_ShareMemory_TC.cu 2 threads with a u64 binary search in global
+    memory), each launched as its driver does, beside this library's count
+    of the same graph.  R-MAT scale 16 (all variants) and 18 (the two
+    shared-memory ones; the atomic variants serialise on one counter).  L2 is
+    flushed before every launch."""
+    import torch
+
+    import oracle
+    import trianglecount_gb300 as tc
+    from trianglecount_gb300 import generators as gen
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    ctx = tc.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    d_out = torch.zeros(1, dtype=torch.int64, device=dev)
+    lib = tc.lib()
+    graphs = {}
+    for scale, variants in ((16, ("tc128", "smem64", "atomic256", "nosmem2")), (18, ("tc128", "smem64"))):
+        src, dst = gen.rmat(scale, 16)
+        g = ctx.graph_from_edges(src, dst)
+        rp, col = g.download()
+        want = ctx.count(g)
+        ours = _timed(stream, flush, lambda: lib.tc_count_async(ctx.handle, g.handle, d_out.data_ptr()),
+                      args.steps, args.warmup)
+        assert int(d_out.item()) == want
+        row = {"V": g.n_rows, "oriented_edges": g.nnz, "triangles": want, "ours_ms": ours}
+        for v in variants:
+            if not oracle.ref_variant_available(v):
+                row[v] = "unavailable: cubin not built (needs the reference tree at build time)"
+                continue
+            total, ms = oracle.ref_variant(v, rp, col, runs=3 if v in ("tc128", "smem64") else 1)
+            row[v] = {"ms": ms, "count_matches": total == want, "speedup_of_ours": ms / ours}
+        graphs[f"rmat{scale}"] = row
+    r16 = graphs["rmat16"]
+    cfg = {"workload": "reference_design_space_study", "graphs": graphs,
+           "variants": {k: {"cubin": c, "threads_per_block": t, "u64": bool(u), "one_atomic_per_probe": bool(a)}
+                        for k, (c, _, t, u, a) in oracle.REF_VARIANTS.items()},
+           "l2": "flushed before every launch (512 MiB memset)"}
+    res = {"metric": METRIC, "value": world * r16["oriented_edges"] / (r16["ours_ms"] / 1000.0), "unit": UNIT,
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r16["ours_ms"],
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+           "data": "synthetic (seeded R-MAT)", "config": cfg}
+    ctx.close()
+    return res
+
+
 def run_parts(args, world, rank, local, pg):
     """Partitioned halo path on R-MAT scale 23: device clean-up, orientation and
     halo extraction for k = 2, 4, 8 seeded random parts; every part counted by
@@ -600,7 +654,8 @@ def main():
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:
-        fn = {"rmat23_parts": run_parts, "batch256": run_batch, "serve": run_serve}.get(args.workload, run_ours)
+        fn = {"rmat23_parts": run_parts, "batch256": run_batch, "serve": run_serve,
+              "refstudy": run_refstudy}.get(args.workload, run_ours)
         res = fn(args, world, rank, local, pg)
         if rank == 0:
             print(json.dumps(res), flush=True)

@@ -146,13 +146,49 @@ def pipeline(src, dst, n_nodes: int = 0, tie="reference"):
 
 
 # ---- the reference's own TC_128 kernel (oracle/_ref, built by build_ref.sh) ----
-REF_CUBIN = os.path.join(_HERE, "_ref", "tc128_sm103a.cubin")
+REF_DIR = os.path.join(_HERE, "_ref")
+REF_CUBIN = os.path.join(REF_DIR, "tc128_sm103a.cubin")
 REF_LAUNCH = os.path.join(_HERE, "_build", "libref_launch.so")
 UNDIR2DIR = os.path.join(_HERE, "_ref", "undir2dir")
 
 
 def ref_kernel_available() -> bool:
     return os.path.exists(REF_CUBIN) and os.path.exists(REF_LAUNCH)
+
+
+# The reference's design-space variants of its Find_Triangle kernel
+# (src/WithoutPartition/): name -> (cubin, kernel symbol, threads per block,
+# u64 indices, adds every hit to one counter).
+REF_VARIANTS = {
+    "tc128": ("tc128_sm103a.cubin", "_Z13Find_TrianglePiS_iiPy", 128, 0, 0),   # ShareKernelTCV62_update_v1.cu
+    "smem64": ("var_smem64_sm103a.cubin", "_Z13Find_TrianglePiS_iiPy", 64, 0, 0),  # shareMemSize.cu
+    "atomic256": ("var_atomic256_sm103a.cubin", "_Z13Find_TrianglePiS_iiPy", 256, 0, 1),  # With_Atomic_op.cu
+    "nosmem2": ("var_nosmem2_sm103a.cubin", "_Z13Find_TrianglePyS_S_", 2, 1, 1),  # Without_ShareMemory_TC.cu
+}
+
+
+def ref_variant_available(name: str) -> bool:
+    return os.path.exists(os.path.join(REF_DIR, REF_VARIANTS[name][0])) and os.path.exists(REF_LAUNCH)
+
+
+def ref_variant(name: str, row_ptr, col, runs: int = 1):
+    """Run one of the reference's kernel variants on cuda:0 with its own launch
+    shape -> (total count, last kernel time in ms)."""
+    cubin, sym, threads, idx64, total_only = REF_VARIANTS[name]
+    L = C.CDLL(REF_LAUNCH)
+    L.ref_variant_run.restype = C.c_int
+    L.ref_variant_run.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                  C.c_int32, C.c_int32, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_float),
+                                  C.c_char_p, C.c_int]
+    rp = np.ascontiguousarray(row_ptr, np.int32)
+    cl = np.ascontiguousarray(col, np.int32)
+    tot, ms = C.c_uint64(), C.c_float()
+    err = C.create_string_buffer(256)
+    rc = L.ref_variant_run(os.path.join(REF_DIR, cubin).encode(), sym.encode(), threads, idx64, total_only, _p(rp),
+                           _p(cl), len(rp) - 1, len(cl), int(runs), C.byref(tot), C.byref(ms), err, 256)
+    if rc != 0:
+        raise RuntimeError(f"reference variant {name} failed: {err.value.decode()}")
+    return int(tot.value), ms.value
 
 
 def ref_tc128(row_ptr, col, runs: int = 1):

@@ -8,6 +8,11 @@
 #                         (TC_128's Find_Triangle) for sm_103a, launched by
 #                         oracle/ref_launch.cu to cross-check counts and time the
 #                         reference kernel on the same GPU
+#   var_*_sm103a.cubin    the reference's design-space variants of the same kernel
+#                         (src/WithoutPartition/): shareMemSize.cu (64 threads),
+#                         With_Atomic_op.cu (256 threads, one atomic per probe),
+#                         Without_ShareMemory_TC.cu (2 threads, u64, binary search
+#                         in global memory) -- timed beside TC_128 on the GB300
 #
 # src/WithPartition/without_sorting_tc.cu (wo_sort_tc_256) is compiled here only
 # to show it builds; its kernel calls __syncthreads() inside `if (tid == 0)`
@@ -21,6 +26,10 @@ mkdir -p "$OUT"
 g++ -O2 -w -x c++ -I "$REF/preprocess_CPU" "$REF/preprocess_CPU/Undir2Dir.c" -o "$OUT/undir2dir"
 "$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a \
     "$REF/src/WithoutPartition/ShareKernelTCV62_update_v1.cu" -o "$OUT/tc128_sm103a.cubin"
+for v in shareMemSize:smem64 With_Atomic_op:atomic256 Without_ShareMemory_TC:nosmem2; do
+    "$NVCC" -cubin -w -gencode arch=compute_103a,code=sm_103a \
+        "$REF/src/WithoutPartition/${v%%:*}.cu" -o "$OUT/var_${v##*:}_sm103a.cubin"
+done
 "$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a \
     "$REF/src/WithPartition/without_sorting_tc.cu" -o "$OUT/wo_sort_sm103a.cubin.unused"
 echo "built $(ls "$OUT" | tr '\n' ' ')"

@@ -34,3 +34,23 @@ def test_per_root_matches_reference_kernel(ctx, maker):
     ours = ctx.count_per_root(g)
     assert np.array_equal(ours, ref_pr)
     assert ctx.count(g) == int(ref_pr.sum())
+
+
+@pytest.mark.parametrize("variant", sorted(oracle.REF_VARIANTS))
+@pytest.mark.parametrize("maker", ["rmat12", "windmill", "complete_300"])
+def test_reference_variants_agree(ctx, variant, maker):
+    """The reference's design-space variants of its kernel (64-thread blocks,
+    one atomic per probe, u64 binary search without shared memory), built
+    from their sources, count what this library counts."""
+    if not oracle.ref_variant_available(variant):
+        pytest.skip(f"{variant} cubin not built")
+    if maker == "rmat12":
+        src, dst = gen.rmat(12)
+    elif maker == "windmill":
+        src, dst, _ = families.windmill(30, 50)
+    else:
+        src, dst, _ = families.complete(300)
+    orp, ocl, want = oracle.pipeline(src, dst)
+    total, ms = oracle.ref_variant(variant, orp, ocl)
+    assert total == want and ms > 0
+    assert ctx.count(ctx.upload(orp, ocl)) == want
