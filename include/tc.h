@@ -272,7 +272,10 @@ TC_API int tc_server_poll(tc_server *s, uint64_t request_id, uint64_t *count, do
 /* As poll, blocking up to timeout_ms (< 0: no limit); TC_E_TIMEOUT after it. */
 TC_API int tc_server_wait(tc_server *s, uint64_t request_id, int64_t timeout_ms, uint64_t *count, double *latency_ms);
 TC_API int tc_server_get_stats(tc_server *s, tc_server_stats *out);
-/* Finishes admitted work, fails requests still queued, frees everything. */
+/* Finishes admitted work, fails requests still queued, frees everything.
+ * After a batch overran batch_timeout_ms, first waits (up to that long again,
+ * at least 5 s) for its kernels; if they are still running, the server's device memory is
+ * left allocated and TC_E_TIMEOUT is returned (the handle is gone either way). */
 TC_API int tc_server_destroy(tc_server *s);
 
 /* ---- host utilities: text files (the reference's on-disk contract) -------- */

@@ -229,6 +229,19 @@ void count_loop(tc_server *s) {
     }
 }
 
+// Waits (bounded) until the stream has no work left; false if it still has
+// work after timeout_ms or reports an error.
+bool stream_drained(cudaStream_t st, int64_t timeout_ms) {
+    const auto t0 = Clock::now();
+    for (;;) {
+        const cudaError_t q = cudaStreamQuery(st);
+        if (q == cudaSuccess) return true;
+        if (q != cudaErrorNotReady) return false;
+        if (Clock::now() - t0 > std::chrono::milliseconds(timeout_ms)) return false;
+        std::this_thread::sleep_for(std::chrono::milliseconds(1));
+    }
+}
+
 int take_result(tc_server *s, Request *r, uint64_t *count, double *latency_ms) {
     if (count) *count = r->count;
     if (latency_ms) *latency_ms = r->latency_ms;
@@ -382,9 +395,18 @@ int tc_server_destroy(tc_server *s) {
     }
     s->prep_thr.join();
     s->count_thr.join();
+    // A batch that overran its watchdog may still be running on the count
+    // stream: its graphs must not be freed under it.  Wait for it (bounded);
+    // if it is still running, leave the device memory allocated.
+    const bool drained = s->fault == TC_OK ||
+                         stream_drained(s->count_ctx->stream, std::max<int64_t>(s->cfg.batch_timeout_ms, 5000));
     for (auto &kv : s->reqs) {
-        if (kv.second->owns_graph && kv.second->g) tc_graph_destroy(kv.second->g);
+        if (drained && kv.second->owns_graph && kv.second->g) tc_graph_destroy(kv.second->g);
         delete kv.second;
+    }
+    if (!drained) {
+        delete s;
+        return set_error(TC_E_TIMEOUT, "a timed-out batch is still running; its device memory was left allocated");
     }
     for (auto &kv : s->cache) tc_graph_destroy(kv.second.g);
     tc_ctx_destroy(s->count_ctx);
