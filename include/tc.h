@@ -176,7 +176,7 @@ TC_API int tc_count_csr_i32(tc_ctx *ctx, const int32_t *row_ptr, const int32_t *
  * the reference.  d_row_ptr / d_col are device arrays of an oriented CSR as in
  * tc_graph_upload_i32 (not validated); roots are rows [0, n_roots); the count
  * is written to the device word d_out in stream order on `stream` (a
- * cudaStream_t, NULL for the default stream).  Scratch is one fixed ~20 MB
+ * cudaStream_t, NULL for the default stream).  Scratch is one fixed ~22 MB
  * device array inside libtc: at most 262,144 rows and 2,097,152 oriented edges
  * (TC_E_RANGE beyond).  Calls share that array, so calls that overlap on the
  * GPU race; the first call on a device sets up that device and should come

@@ -244,7 +244,7 @@ void ctx_release(tc_ctx *c) {
 int scratch_alloc(CountScratch *sc, int64_t V, int64_t C, int64_t E, int64_t heavy_cap, cudaStream_t s) {
     sc->heavy_cap = heavy_cap;
     TC_TRY(dalloc((void **)&sc->heavy, sizeof(HeavyEntry) * (size_t)std::max<int64_t>(heavy_cap, 1), s));
-    TC_TRY(dalloc((void **)&sc->light_mask, sizeof(uint32_t) * (size_t)std::max<int64_t>(C, 1), s));
+    TC_TRY(dalloc((void **)&sc->light_list, sizeof(uint32_t) * (size_t)std::max<int64_t>(V, 1), s));
     TC_TRY(dalloc((void **)&sc->micro_mask, sizeof(uint32_t) * (size_t)std::max<int64_t>(C, 1), s));
     TC_TRY(dalloc((void **)&sc->in_cnt, sizeof(int32_t) * (size_t)std::max<int64_t>(V, 1), s));
     TC_TRY(dalloc((void **)&sc->in_off, sizeof(int32_t) * (size_t)(V + 1), s));
@@ -257,7 +257,7 @@ int scratch_alloc(CountScratch *sc, int64_t V, int64_t C, int64_t E, int64_t hea
 
 void scratch_free(CountScratch *sc, cudaStream_t s) {
     dfree(sc->heavy, s);
-    dfree(sc->light_mask, s);
+    dfree(sc->light_list, s);
     dfree(sc->micro_mask, s);
     dfree(sc->in_cnt, s);
     dfree(sc->in_off, s);

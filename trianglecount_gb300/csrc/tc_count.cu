@@ -67,6 +67,7 @@ constexpr int kLaneRowDeg = 16; // auxiliary passes: rows with d+ <= this are wa
 constexpr int kMicroDeg = 8;    // micro tasks: d+(x) <= this (N+(x) held in registers) ...
 constexpr int kMicroWork = 512; // ... and at most this many probes (one lane runs the task)
 constexpr int kAuxGrab = 4;     // 32-row chunks an auxiliary-kernel warp takes per cursor grab
+constexpr int kLightGrab = 4;   // light tasks a count-kernel warp takes per cursor grab
 constexpr int kMinUnit = 8192;  // smallest heavy block unit (probes)
 constexpr int kMinLight = 1024; // smallest light-task bound (probes)
 #ifndef TC_COUNT_MIN_BLOCKS
@@ -245,7 +246,7 @@ struct KParams {
     int64_t heavy_cap;
     CountWork *work;
     unsigned long long *results;
-    uint32_t *light_mask;  // one word per 32-row chunk
+    uint32_t *light_list;  // light tasks (chunk * 32 + lane), work->n_light of them
     uint32_t *micro_mask;  // one word per 32-row chunk
     int32_t *in_cnt;       // per vertex (pooled): middle-centric in-edges, consumed by the transpose
     int32_t *in_off;       // per vertex (pooled) + 1: exclusive scan of in_cnt
@@ -548,9 +549,12 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
             const bool hv = has && !micro && !light;
             const uint32_t mm = __ballot_sync(kFull, micro);
             const uint32_t lm = __ballot_sync(kFull, light);
-            if (lane == 0) {
-                P.light_mask[c] = lm;
-                P.micro_mask[c] = mm;
+            if (lane == 0) P.micro_mask[c] = mm;
+            if (lm) {  // list the chunk's light tasks (one atomic per chunk)
+                unsigned base = 0;
+                if (lane == 0) base = atomicAdd(&P.work->n_light, (unsigned)__popc(lm));
+                base = __shfl_sync(kFull, base, 0);
+                if (light) P.light_list[base + __popc(lm & ((1u << lane) - 1u))] = (uint32_t)(c * kWarp + lane);
             }
             unsigned hm = __ballot_sync(kFull, hv);
             while (hm) {
@@ -961,34 +965,39 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
     }
 
     // ---- phase B: light tasks, one warp each ----
+    // Warps take kLightGrab tasks at a time from the classifier's list, so the
+    // last tasks of the kernel are single tasks, not whole 32-row chunks.
     int *wtab = smem + warp * (1 << P.log_warp_slots);
+    const unsigned n_light = P.work->n_light;
     for (;;) {
-        unsigned c = 0;
-        if (lane == 0) c = atomicAdd(&P.work->small_cursor, 1u);
-        c = __shfl_sync(kFull, c, 0);
-        if ((int64_t)c >= P.total_chunks) break;
-        unsigned todo = P.light_mask[c];
-        if (!todo) continue;
-        const int g = find_graph(P.gd, P.n_graphs, c);
-        const GraphDesc &G = P.gd[g];
-        const int32_t *__restrict__ rp = G.rp;
-        const int32_t *__restrict__ col = G.col;
-        if (!kPerRoot && g != cur_g) flush(g);
-        const int64_t x0 = ((int64_t)c - G.chunk_base) * kWarp;
-        int rs = 0, d = 0, i0 = 0, i1 = 0;
-        if ((todo >> lane) & 1u) {
-            rs = __ldg(rp + x0 + lane);
-            d = __ldg(rp + x0 + lane + 1) - rs;
-            i0 = P.in_off[G.vbase + x0 + lane];
-            i1 = P.in_off[G.vbase + x0 + lane + 1];
+        unsigned t0 = 0;
+        if (lane == 0) t0 = atomicAdd(&P.work->small_cursor, (unsigned)kLightGrab);
+        t0 = __shfl_sync(kFull, t0, 0);
+        if (t0 >= n_light) break;
+        const int nt = (int)min((unsigned)kLightGrab, n_light - t0);
+        // the grabbed tasks' rows, one lane each
+        int rs = 0, d = 0, i0 = 0, i1 = 0, tg = 0, tx = 0;
+        if (lane < nt) {
+            const uint32_t gi = P.light_list[t0 + lane];
+            const int64_t c = (int64_t)(gi / kWarp);
+            tg = find_graph(P.gd, P.n_graphs, c);
+            const GraphDesc &Gl = P.gd[tg];
+            tx = (int)((c - Gl.chunk_base) * kWarp + (int64_t)(gi % kWarp));
+            rs = __ldg(Gl.rp + tx);
+            d = __ldg(Gl.rp + tx + 1) - rs;
+            i0 = P.in_off[Gl.vbase + tx];
+            i1 = P.in_off[Gl.vbase + tx + 1];
         }
-        while (todo) {
-            const int k = __ffs(todo) - 1;
-            todo &= todo - 1u;
+        for (int k = 0; k < nt; ++k) {
+            const int g = __shfl_sync(kFull, tg, k);
+            const GraphDesc &G = P.gd[g];
+            const int32_t *__restrict__ rp = G.rp;
+            const int32_t *__restrict__ col = G.col;
+            if (!kPerRoot && g != cur_g) flush(g);
             Task T;
             const int rrs = __shfl_sync(kFull, rs, k);
             T.dx = __shfl_sync(kFull, d, k);
-            T.x = (int)(x0 + k);
+            T.x = __shfl_sync(kFull, tx, k);
             T.n_out = T.x < G.n_roots ? T.dx : 0;
             T.out_nbr = col + rrs;
             const int ri0 = __shfl_sync(kFull, i0, k);
@@ -1106,7 +1115,7 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
     P.heavy_cap = sc.heavy_cap;
     P.work = work;
     P.results = results;
-    P.light_mask = sc.light_mask;
+    P.light_list = sc.light_list;
     P.micro_mask = sc.micro_mask;
     P.in_cnt = sc.in_cnt;
     P.in_off = sc.in_off;
@@ -1128,6 +1137,9 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
     const bool bitmap = tn.heavy_bitmap && bitmap_words > 0 && bitmap_words * 4 <= (int64_t)tn.bitmap_bytes;
     P.heavy_done = bitmap ? 1 : 0;
     if (bitmap) P.tile = INT32_MAX / 2;  // one tile: the bitmap has no capacity limit
+    // light tasks are listed as 32-bit global row indices
+    if (total_chunks * kWarp >= ((int64_t)1 << 32))
+        return set_error(TC_E_RANGE, "a count of more than 2^32 rows in one launch is not supported");
     TC_CUDA(cudaMemsetAsync(work, 0, sizeof(CountWork), s));
     TC_CUDA(cudaMemsetAsync(results, 0, sizeof(unsigned long long) * (size_t)n_graphs, s));
     int nl = 0;
@@ -1204,7 +1216,7 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
     P.heavy_cap = sc.heavy_cap;
     P.work = work;
     P.results = results;
-    P.light_mask = sc.light_mask;
+    P.light_list = sc.light_list;
     P.micro_mask = sc.micro_mask;
     P.in_cnt = sc.in_cnt;
     P.in_off = sc.in_off;

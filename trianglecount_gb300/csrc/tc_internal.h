@@ -84,7 +84,7 @@ struct HeavyEntry {
 struct CountScratch {
     HeavyEntry *heavy = nullptr;  // heavy_cap entries
     int64_t heavy_cap = 0;
-    uint32_t *light_mask = nullptr;         // C words
+    uint32_t *light_list = nullptr;         // V: light tasks, as global row index chunk * 32 + lane
     uint32_t *micro_mask = nullptr;         // C words
     int32_t *in_cnt = nullptr;              // V
     int32_t *in_off = nullptr;              // V + 1
@@ -100,10 +100,12 @@ void scratch_free(CountScratch *sc, cudaStream_t s);
 struct CountWork {
     unsigned long long heavy_packed; // (entries << 32) | units, from the classifier
     unsigned int heavy_cursor;
-    unsigned int small_cursor;
+    unsigned int small_cursor;       // light-task cursor
     unsigned int aux_cursor[3];      // chunk cursors of in_count, transpose/classify, micro
     int error;
     unsigned long long total_work;   // sum over oriented edges of the cheaper side's length
+    unsigned int n_light;            // light tasks listed by the classifier
+    unsigned int pad;
 };
 
 struct Tuned {  // resolved tc_tuning with derived table geometry

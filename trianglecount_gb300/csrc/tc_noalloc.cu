@@ -7,7 +7,7 @@
 // host denies allocations.  tc_count_noalloc_i32 serves them: the caller hands
 // in device pointers to the oriented CSR and to the 8-byte result, and every
 // scratch array the count needs lives in one file-scope device array of fixed
-// size (kScratchBytes below, about 20 MB), which each GPU that loads libtc
+// size (kScratchBytes below, about 22 MB), which each GPU that loads libtc
 // keeps until the process exits.
 //
 // Limits: n_rows <= kMaxRows (262,144) and nnz <= kMaxNnz (2,097,152); larger
@@ -36,7 +36,7 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t kOffWork = 0;  // CountWork + 8-byte result
 constexpr size_t kOffDesc = align256(kOffWork + sizeof(CountWork) + 8);
 constexpr size_t kOffMask = align256(kOffDesc + sizeof(GraphDesc));
-constexpr size_t kOffMicro = align256(kOffMask + sizeof(uint32_t) * (kMaxRows / 32 + 1));
+constexpr size_t kOffMicro = align256(kOffMask + sizeof(uint32_t) * (kMaxRows + 1));
 constexpr size_t kOffHeavy = align256(kOffMicro + sizeof(uint32_t) * (kMaxRows / 32 + 1));
 constexpr size_t kOffInCnt = align256(kOffHeavy + sizeof(HeavyEntry) * (kMaxRows + 1));
 constexpr size_t kOffInOff = align256(kOffInCnt + sizeof(int32_t) * (kMaxRows + 1));
@@ -114,7 +114,7 @@ extern "C" int tc_count_noalloc_i32(const int32_t *d_row_ptr, const int32_t *d_c
     CountScratch sc;
     sc.heavy = (HeavyEntry *)(base + kOffHeavy);
     sc.heavy_cap = std::min(n_rows, nnz) + 1;
-    sc.light_mask = (uint32_t *)(base + kOffMask);
+    sc.light_list = (uint32_t *)(base + kOffMask);
     sc.micro_mask = (uint32_t *)(base + kOffMicro);
     sc.in_cnt = (int32_t *)(base + kOffInCnt);
     sc.in_off = (int32_t *)(base + kOffInOff);
