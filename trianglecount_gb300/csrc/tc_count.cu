@@ -21,24 +21,29 @@
 // u with d+(u) < d+(x) (u a root).  The in-neighbour lists are a transpose of
 // the middle-centric edges built on the device for every count.
 //
+// A graph with no row longer than flat_max_deg (8) is counted instead by one
+// flat_kernel: one lane per root, N+(u) and every N+(v) in registers.
+//
 // Launch sequence (one CUDA-graph-capturable chain, plain or batched):
-//   in_count   one warp per 32 rows: per root u, per v in N+(u), count the
-//              middle-centric in-edges of v and their work; the root-centric
-//              work of u
+//   in_count   one warp per 32 rows: per root u, per v in N+(u), mark the edge
+//              middle-centric or not, count the middle-centric in-edges of v
+//              and their work, the root-centric work of u, and the total
 //   scan       in-edge offsets
 //   transpose  per root u, scatter the middle-centric edges into the in-lists;
-//              classify each vertex x by d+(x) and its work w(x): light tasks
-//              (d+(x) <= warp_max, w(x) <= light_max_work) are marked in a
-//              32-bit mask per chunk; heavy ones become (#tiles x #slices)
+//              classify each vertex x by d+(x) and its work w(x): micro tasks
+//              (d+(x) <= 8, w(x) <= 512) are marked in a 32-bit mask per
+//              chunk, light tasks (d+(x) <= warp_max, w(x) <= the light bound)
+//              are appended to a list, heavy ones become (#tiles x #slices)
 //              block units, appended with one packed 64-bit atomic so entries
 //              stay sorted by unit
+//   micro      one lane per micro task, N+(x) in registers
 //   count      persistent grid (SMs x occupancy blocks):
 //                phase A -- blocks pull heavy units from a global cursor; a
 //                  unit hashes one tile of N+(x) (load factor <= 1/4) in shared
 //                  memory and its warps pull 16-partner chunks of the unit's
 //                  slice from a shared cursor;
-//                phase B -- each warp pulls 32-row chunks and runs the light
-//                  tasks of the chunk with a per-warp shared hash.
+//                phase B -- warps take light tasks four at a time from the
+//                  list and run each with a per-warp shared hash.
 //              Streaming a chunk of partners: lists with length >= long_list are
 //              read by the whole warp, four coalesced loads in flight per lane;
 //              shorter lists are flattened across the lanes (warp scan of the
