@@ -31,7 +31,7 @@
 //   scan       in-edge offsets
 //   transpose  per root u, scatter the middle-centric edges into the in-lists;
 //              classify each vertex x by d+(x) and its work w(x): micro tasks
-//              (d+(x) <= 8, w(x) <= 512) are marked in a 32-bit mask per
+//              (d+(x) <= 8, w(x) <= 128) are marked in a 32-bit mask per
 //              chunk, light tasks (d+(x) <= warp_max, w(x) <= the light bound)
 //              are appended to a list, heavy ones become (#tiles x #slices)
 //              block units, appended with one packed 64-bit atomic so entries
@@ -70,7 +70,7 @@ constexpr int kWarpsPerBlock = kThreads / kWarp;
 constexpr int kHeavyChunk = 16; // partners per warp grab inside a heavy unit (4: R-MAT 21 kernel 6.49 ms, 16: 6.04)
 constexpr int kLaneRowDeg = 16; // auxiliary passes: rows with d+ <= this are walked one per lane
 constexpr int kMicroDeg = 8;    // micro tasks: d+(x) <= this (N+(x) held in registers) ...
-constexpr int kMicroWork = 512; // ... and at most this many probes (one lane runs the task)
+constexpr int kMicroWork = 128; // ... and at most this many probes (one lane runs the task serially)
 constexpr int kAuxGrab = 4;     // 32-row chunks an auxiliary-kernel warp takes per cursor grab
 constexpr int kLightGrab = 4;   // light tasks a count-kernel warp takes per cursor grab
 constexpr int kMinUnit = 8192;  // smallest heavy block unit (probes)
