@@ -353,7 +353,8 @@ def run_ours(args, world, rank, local, pg):
                          "traffic_source": (tr or {}).get("source")},
             "clocks": clk,
         }
-        if not args.no_ref_kernel:
+        # the CPU and reference-kernel baselines are taken at N = 1 only
+        if not args.no_ref_kernel and world == 1:
             try:
                 import oracle
                 if oracle.ref_kernel_available():
@@ -373,7 +374,7 @@ def run_ours(args, world, rank, local, pg):
                         "speedup_of_ours": rms / ms}
             except Exception as ex:  # reported, never fatal
                 res["reference_gpu_kernel"] = {"unavailable": str(ex)[:200]}
-        if not args.no_cpu:
+        if not args.no_cpu and world == 1:
             import oracle
             t0 = time.perf_counter()
             ccount = oracle.count(rp, col)
