@@ -4,6 +4,8 @@
   rmat_counts.json       counts of seeded R-MAT graphs (scales 8..14) from the
                          CPU oracle; the generator draws integers only, so these
                          pin the generator + pipeline on every platform
+  fullsize_counts.json   the same for the benchmark-size workloads (R-MAT 21,
+                         road 1448 x 1448, R-MAT 23)
   undir2dir_*.npz        orientation golden vectors produced by the reference's
                          own CPU converter (preprocess_CPU/Undir2Dir.c, built by
                          oracle/build_ref.sh into oracle/_ref/undir2dir) on small
@@ -51,6 +53,24 @@ def rmat_counts():
         json.dump(out, f, indent=1)
 
 
+def fullsize_counts():
+    """Counts of the benchmark-size workloads (R-MAT scale 21 and 23 with their
+    default seeds, the 1448 x 1448 road grid), from the CPU oracle: the GPU
+    tests compare the device counts and the halo-part sums with these."""
+    out = {}
+    cases = {"rmat21": lambda: gen.rmat(21, 16), "road": lambda: gen.road(), "rmat23": lambda: gen.rmat(23, 16)}
+    for name, make in cases.items():
+        src, dst = make()
+        rp, col = oracle.clean(src, dst)
+        orp, ocl = oracle.orient(rp, col)
+        out[name] = {"V": len(rp) - 1, "undirected_nnz": len(col), "oriented_nnz": len(ocl),
+                     "triangles": oracle.count(orp, ocl),
+                     "edge_checksum": int((src * 1000003 + dst).sum() % (1 << 61))}
+        print(name, out[name], flush=True)
+    with open(os.path.join(HERE, "fullsize_counts.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
 def undir2dir_goldens():
     exe = oracle.UNDIR2DIR
     if not os.path.exists(exe):
@@ -84,5 +104,7 @@ def undir2dir_goldens():
 if __name__ == "__main__":
     known_graphs()
     rmat_counts()
+    if "--fullsize" in sys.argv:  # minutes of CPU time
+        fullsize_counts()
     undir2dir_goldens()
     print("golden fixtures written to", HERE)

@@ -1,0 +1,63 @@
+"""Parity at the benchmark sizes: R-MAT scale 21 and the 1448 x 1448 road grid
+(plain path, both counting paths), R-MAT scale 23 whole and in k = 2, 4, 8
+random halo parts (sum of parts == whole, batched == per part), against the
+CPU oracle's counts committed in tests/golden/fullsize_counts.json."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import trianglecount_gb300 as tc
+from trianglecount_gb300 import generators as gen
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def full(golden_dir):
+    return json.load(open(os.path.join(golden_dir, "fullsize_counts.json")))
+
+
+def test_rmat21_plain_per_root_and_batched(ctx, full):
+    want = full["rmat21"]
+    g = ctx.graph_from_edges(*gen.rmat(21, 16))
+    assert (g.n_rows, g.nnz) == (want["V"], want["oriented_nnz"])
+    assert ctx.count(g) == want["triangles"]
+    pr = ctx.count_per_root(g)
+    assert int(pr.sum()) == want["triangles"] and len(pr) == g.n_roots
+    b = ctx.batch([g, g])
+    assert list(b.run()) == [want["triangles"]] * 2
+    b.free()
+
+
+def test_road_flat_and_chain(ctx, full):
+    want = full["road"]
+    g = ctx.graph_from_edges(*gen.road())
+    assert (g.n_rows, g.nnz) == (want["V"], want["oriented_nnz"])
+    old = ctx.get_tuning()
+    try:
+        got, st = ctx.count(g, stats=True)
+        assert got == want["triangles"] and st["launches"] == 1  # one flat kernel
+        ctx.set_tuning(flat_max_deg=0)
+        got, st = ctx.count(g, stats=True)
+        assert got == want["triangles"] and st["launches"] >= 4  # the full chain
+    finally:
+        ctx.set_tuning(flat_max_deg=old["flat_max_deg"])
+
+
+def test_rmat23_halo_parts_sum_to_whole(ctx, full):
+    want = full["rmat23"]
+    ug = ctx.ugraph_from_edges(*gen.rmat(23, 16))
+    og = ctx.orient(ug)
+    assert (og.n_rows, og.nnz) == (want["V"], want["oriented_nnz"])
+    assert ctx.count(og) == want["triangles"]
+    for k in (2, 4, 8):
+        parts = ctx.halo_extract(ug, gen.parts_random(og.n_rows, k), k)
+        each = ctx.count_each(parts)
+        assert int(each.sum()) == want["triangles"], k
+        b = ctx.batch(parts)
+        assert np.array_equal(b.run(), each), k
+        b.free()
+        for p in parts:
+            p.free()

@@ -134,3 +134,13 @@ def test_planted_orientation_mistake_is_caught():
     orp = np.concatenate([[0], np.cumsum([len(k) for k in keep])])
     ocl = np.concatenate(keep).astype(np.int64)
     assert oracle.count(orp, ocl) != families.expected("complete", [12])
+
+
+def test_fullsize_generators_are_pinned(golden_dir):
+    """The benchmark-size inputs (R-MAT 21 / 23, road 1448 x 1448) are drawn
+    with integer-only generators: their edge checksums match the committed
+    ones on every platform, so the full-size golden counts apply."""
+    full = json.load(open(os.path.join(golden_dir, "fullsize_counts.json")))
+    for name, make in (("rmat21", lambda: gen.rmat(21, 16)), ("road", gen.road), ("rmat23", lambda: gen.rmat(23, 16))):
+        src, dst = make()
+        assert int((src * 1000003 + dst).sum() % (1 << 61)) == full[name]["edge_checksum"], name
