@@ -72,6 +72,10 @@ constexpr int kLaneRowDeg = 16; // auxiliary passes: rows with d+ <= this are wa
 constexpr int kMicroDeg = 8;    // micro tasks: d+(x) <= this (N+(x) held in registers) ...
 constexpr int kMicroWork = 128; // ... and at most this many probes (one lane runs the task serially)
 constexpr int kAuxGrab = 4;     // 32-row chunks an auxiliary-kernel warp takes per cursor grab
+// One middle-centric in-edge in a packed in_work word.  Both halves stay below
+// 2^31: a vertex has fewer than nnz in-edges, and its in-partners' d+(u) sum to
+// at most nnz < 2^31 (each u counted once), so one 64-bit atomic adds both.
+constexpr unsigned long long kInEdge = 1ull << 32;
 constexpr int kLightGrab = 4;   // light tasks a count-kernel warp takes per cursor grab
 constexpr int kMinUnit = 8192;  // smallest heavy block unit (probes)
 constexpr int kMinLight = 1024; // smallest light-task bound (probes)
@@ -253,9 +257,10 @@ struct KParams {
     unsigned long long *results;
     uint32_t *light_list;  // light tasks (chunk * 32 + lane), work->n_light of them
     uint32_t *micro_mask;  // one word per 32-row chunk
-    int32_t *in_cnt;       // per vertex (pooled): middle-centric in-edges, consumed by the transpose
+    int32_t *in_cnt;       // per vertex (pooled): middle-centric in-edges (split from in_work)
     int32_t *in_off;       // per vertex (pooled) + 1: exclusive scan of in_cnt
-    unsigned long long *in_work;   // per vertex: sum of d+(u) over its in-partners u
+    unsigned long long *in_work;   // per vertex: (in-edges << 32) | sum of d+(u) over its in-partners u;
+                                   // the transpose counts the high half back down
     unsigned long long *out_work;  // per vertex: sum of d+(v) over its out-partners v
     int32_t *in_list;      // in-partner lists, in_off-indexed
     uint8_t *mid;          // per oriented edge (pooled by ebase): 1 = middle-centric
@@ -446,8 +451,7 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
                         const bool m = d < dv[q];
                         P.mid[G.ebase + rs + i0 + q] = (uint8_t)m;
                         if (m) {
-                            atomicAdd(P.in_cnt + G.vbase + v[q], 1);
-                            atomicAdd(P.in_work + G.vbase + v[q], (unsigned long long)d);
+                            atomicAdd(P.in_work + G.vbase + v[q], kInEdge | (unsigned long long)d);
                             probes += (unsigned long long)d;
                         } else {
                             ow += (unsigned long long)dv[q];
@@ -471,8 +475,7 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
                     const bool m = rd < dv;
                     P.mid[G.ebase + rrs + i] = (uint8_t)m;
                     if (m) {
-                        atomicAdd(P.in_cnt + G.vbase + v, 1);
-                        atomicAdd(P.in_work + G.vbase + v, (unsigned long long)rd);
+                        atomicAdd(P.in_work + G.vbase + v, kInEdge | (unsigned long long)rd);
                         probes += (unsigned long long)rd;
                     } else {
                         ow += (unsigned long long)dv;
@@ -487,6 +490,14 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
     // every edge's probes (the cheaper side) once, for the classifier's unit size
     probes = warp_sum_u64(probes);
     if (lane == 0 && probes) atomicAdd(&P.work->total_work, probes);
+}
+
+// in_cnt[i] = the in-edge count (high half) of the packed in_work[i], for the scan.
+__global__ void __launch_bounds__(kThreads) split_in_count_kernel(const unsigned long long *__restrict__ in_work,
+                                                                  int32_t *__restrict__ in_cnt, int64_t n) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        in_cnt[i] = (int32_t)(in_work[i] >> 32);
 }
 
 // transpose + classify: scatter the chunk's middle-centric edges into the
@@ -521,7 +532,7 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
                 rs = __ldg(rp + x);
                 d = __ldg(rp + x + 1) - rs;
                 nin = P.in_off[G.vbase + x + 1] - P.in_off[G.vbase + x];
-                w = P.out_work[G.vbase + x] + P.in_work[G.vbase + x];
+                w = P.out_work[G.vbase + x] + (P.in_work[G.vbase + x] & 0xffffffffull);
             }
             // scatter the middle-centric out-edges of the chunk's roots (marked by
             // in_count): short rows one per lane ...
@@ -529,7 +540,7 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
                 for (int i = 0; i < d; ++i) {
                     if (!P.mid[G.ebase + rs + i]) continue;
                     const int v = __ldg(col + rs + i);
-                    const int pos = atomicSub(P.in_cnt + G.vbase + v, 1) - 1;
+                    const int pos = (int)(atomicAdd(P.in_work + G.vbase + v, 0ull - kInEdge) >> 32) - 1;
                     P.in_list[P.in_off[G.vbase + v] + pos] = (int32_t)x;
                 }
             }
@@ -543,7 +554,7 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
                 for (int i = lane; i < rd; i += kWarp) {
                     if (!P.mid[G.ebase + rrs + i]) continue;
                     const int v = __ldg(col + rrs + i);
-                    const int pos = atomicSub(P.in_cnt + G.vbase + v, 1) - 1;
+                    const int pos = (int)(atomicAdd(P.in_work + G.vbase + v, 0ull - kInEdge) >> 32) - 1;
                     P.in_list[P.in_off[G.vbase + v] + pos] = (int32_t)(x0 + k);
                 }
             }
@@ -1149,7 +1160,6 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
     TC_CUDA(cudaMemsetAsync(results, 0, sizeof(unsigned long long) * (size_t)n_graphs, s));
     int nl = 0;
     if (total_chunks > 0) {
-        TC_CUDA(cudaMemsetAsync(sc.in_cnt, 0, sizeof(int32_t) * (size_t)total_vertices, s));
         TC_CUDA(cudaMemsetAsync(sc.in_work, 0, sizeof(unsigned long long) * (size_t)total_vertices, s));
         TC_CUDA(cudaMemsetAsync(sc.out_work, 0, sizeof(unsigned long long) * (size_t)total_vertices, s));
         const int64_t want = (total_chunks + kWarpsPerBlock - 1) / kWarpsPerBlock;
@@ -1157,6 +1167,9 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
         const int64_t cap = P.aux_dynamic ? (int64_t)tn.aux_blocks : (int64_t)tn.blocks * 4;
         const int aux_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, cap));
         in_count_kernel<<<aux_blocks, kThreads, 0, s>>>(P);
+        TC_CUDA(cudaGetLastError());
+        split_in_count_kernel<<<(int)std::min<int64_t>((total_vertices + kThreads - 1) / kThreads, (int64_t)tn.blocks * 4),
+                                kThreads, 0, s>>>(sc.in_work, sc.in_cnt, total_vertices);
         TC_CUDA(cudaGetLastError());
         TC_TRY(scan_exclusive_i32(sc.in_cnt, sc.in_off, total_vertices, s));
         transpose_classify_kernel<<<aux_blocks, kThreads, 0, s>>>(P, sc.heavy);
@@ -1180,7 +1193,7 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
         }
         if (kev) TC_CUDA(cudaEventRecord(kev[1], s));
         TC_CUDA(cudaGetLastError());
-        nl += 4 + (total_vertices > 4096 ? 3 : 1);
+        nl += 5 + (total_vertices > 4096 ? 3 : 1);
     }
     if (launches) *launches = nl;
     return TC_OK;
@@ -1242,13 +1255,15 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
     TC_CUDA(cudaMemsetAsync(work, 0, sizeof(CountWork), s));
     TC_CUDA(cudaMemsetAsync(results, 0, sizeof(unsigned long long), s));
     if (total_chunks > 0) {
-        TC_CUDA(cudaMemsetAsync(sc.in_cnt, 0, sizeof(int32_t) * (size_t)total_vertices, s));
         TC_CUDA(cudaMemsetAsync(sc.in_work, 0, sizeof(unsigned long long) * (size_t)total_vertices, s));
         TC_CUDA(cudaMemsetAsync(sc.out_work, 0, sizeof(unsigned long long) * (size_t)total_vertices, s));
         const int64_t want = (total_chunks + kWarpsPerBlock - 1) / kWarpsPerBlock;
         P.aux_dynamic = 0;
         const int aux_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)tn.blocks * 4));
         in_count_kernel<<<aux_blocks, kThreads, 0, s>>>(P);
+        TC_CUDA(cudaGetLastError());
+        split_in_count_kernel<<<(int)std::min<int64_t>((total_vertices + kThreads - 1) / kThreads, (int64_t)tn.blocks * 4),
+                                kThreads, 0, s>>>(sc.in_work, sc.in_cnt, total_vertices);
         TC_CUDA(cudaGetLastError());
         TC_TRY(scan_exclusive_i32_tmp(sc.in_cnt, sc.in_off, total_vertices, scan_tmp, scan_tmp_cap, s));
         transpose_classify_kernel<<<aux_blocks, kThreads, 0, s>>>(P, sc.heavy);
