@@ -257,7 +257,7 @@ struct KParams {
     unsigned long long *results;
     uint32_t *light_list;  // light tasks (chunk * 32 + lane), work->n_light of them
     uint32_t *micro_mask;  // one word per 32-row chunk
-    int32_t *in_cnt;       // per vertex (pooled): middle-centric in-edges (split from in_work)
+    int32_t *in_cnt;       // per vertex (pooled): d+ during in_count, then middle-centric in-edges (split from in_work)
     int32_t *in_off;       // per vertex (pooled) + 1: exclusive scan of in_cnt
     unsigned long long *in_work;   // per vertex: (in-edges << 32) | sum of d+(u) over its in-partners u;
                                    // the transpose counts the high half back down
@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
 #pragma unroll
                     for (int q = 0; q < 4; ++q) v[q] = i0 + q < d ? __ldg(col + rs + i0 + q) : -1;
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) dv[q] = v[q] >= 0 ? __ldg(rp + v[q] + 1) - __ldg(rp + v[q]) : 0;
+                    for (int q = 0; q < 4; ++q) dv[q] = v[q] >= 0 ? __ldg(P.in_cnt + G.vbase + v[q]) : 0;
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
                         if (v[q] < 0) continue;
@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
                 unsigned long long ow = 0;
                 for (int i = lane; i < rd; i += kWarp) {
                     const int v = __ldg(col + rrs + i);
-                    const int dv = __ldg(rp + v + 1) - __ldg(rp + v);
+                    const int dv = __ldg(P.in_cnt + G.vbase + v);
                     const bool m = rd < dv;
                     P.mid[G.ebase + rrs + i] = (uint8_t)m;
                     if (m) {
@@ -490,6 +490,19 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
     // every edge's probes (the cheaper side) once, for the classifier's unit size
     probes = warp_sum_u64(probes);
     if (lane == 0 && probes) atomicAdd(&P.work->total_work, probes);
+}
+
+// in_cnt[vbase + x] = d+(x) for every row, for in_count's gathers (one load
+// per edge instead of a row_ptr pair); in_cnt is free until the split below.
+__global__ void __launch_bounds__(kThreads) degree_kernel(KParams P) {
+    const int lane = threadIdx.x & (kWarp - 1);
+    const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / kWarp;
+    for (int64_t c = gwarp; c < P.total_chunks; c += nwarps) {
+        const GraphDesc &G = P.gd[find_graph(P.gd, P.n_graphs, c)];
+        const int64_t x = (c - G.chunk_base) * kWarp + lane;
+        if (x < G.n_rows) P.in_cnt[G.vbase + x] = __ldg(G.rp + x + 1) - __ldg(G.rp + x);
+    }
 }
 
 // in_cnt[i] = the in-edge count (high half) of the packed in_work[i], for the scan.
@@ -1166,6 +1179,8 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
         P.aux_dynamic = n_graphs > 1 ? 1 : 0;
         const int64_t cap = P.aux_dynamic ? (int64_t)tn.aux_blocks : (int64_t)tn.blocks * 4;
         const int aux_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, cap));
+        degree_kernel<<<aux_blocks, kThreads, 0, s>>>(P);
+        TC_CUDA(cudaGetLastError());
         in_count_kernel<<<aux_blocks, kThreads, 0, s>>>(P);
         TC_CUDA(cudaGetLastError());
         split_in_count_kernel<<<(int)std::min<int64_t>((total_vertices + kThreads - 1) / kThreads, (int64_t)tn.blocks * 4),
@@ -1193,7 +1208,7 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
         }
         if (kev) TC_CUDA(cudaEventRecord(kev[1], s));
         TC_CUDA(cudaGetLastError());
-        nl += 5 + (total_vertices > 4096 ? 3 : 1);
+        nl += 6 + (total_vertices > 4096 ? 3 : 1);
     }
     if (launches) *launches = nl;
     return TC_OK;
@@ -1260,6 +1275,8 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
         const int64_t want = (total_chunks + kWarpsPerBlock - 1) / kWarpsPerBlock;
         P.aux_dynamic = 0;
         const int aux_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)tn.blocks * 4));
+        degree_kernel<<<aux_blocks, kThreads, 0, s>>>(P);
+        TC_CUDA(cudaGetLastError());
         in_count_kernel<<<aux_blocks, kThreads, 0, s>>>(P);
         TC_CUDA(cudaGetLastError());
         split_in_count_kernel<<<(int)std::min<int64_t>((total_vertices + kThreads - 1) / kThreads, (int64_t)tn.blocks * 4),
