@@ -25,9 +25,12 @@
 // flat_kernel: one lane per root, N+(u) and every N+(v) in registers.
 //
 // Launch sequence (one CUDA-graph-capturable chain, plain or batched):
+//   degree     d+(x) of every row into a per-vertex array (in_cnt's storage)
 //   in_count   one warp per 32 rows: per root u, per v in N+(u), mark the edge
 //              middle-centric or not, count the middle-centric in-edges of v
-//              and their work, the root-centric work of u, and the total
+//              and their work (one packed atomic), the root-centric work of u,
+//              and the total
+//   split      in-edge counts out of the packed words
 //   scan       in-edge offsets
 //   transpose  per root u, scatter the middle-centric edges into the in-lists;
 //              classify each vertex x by d+(x) and its work w(x): micro tasks
