@@ -87,10 +87,13 @@ TC_API int tc_ctx_device_info(tc_ctx *ctx, int *sm_count, size_t *free_bytes, si
 
 /* Strategy thresholds of the counting kernel (picked by the autotuner).
  * The classifier computes, per vertex task x, d+(x) and its work (the probes
- * of its partners' lists).  Light tasks (d+(x) <= warp_max_deg and work <=
- * light_max_work) run on one warp with a per-warp shared-memory hash of
+ * of its partners' lists).  Micro tasks (d+(x) <= 8, work <= 128) run on one
+ * lane with N+(x) in registers.  Light tasks (d+(x) <= warp_max_deg and work
+ * <= light_max_work) run on one warp with a per-warp shared-memory hash of
  * N+(x); heavy ones are split into block units of about unit_work probes over
- * a shared hash of one tile of N+(x).  Per partner, lists with length >=
+ * a shared hash of one tile of N+(x).  light_max_work and unit_work are upper
+ * bounds: on a small job both are lowered so that every warp / block gets
+ * about four tasks / units (a large one would be the kernel's tail).  Per partner, lists with length >=
  * long_list are streamed by the whole warp; shorter lists are flattened
  * across the lanes.  probe_kicks > 0 selects a cuckoo hash (two fixed probe
  * slots per lookup, at most probe_kicks displacements per insertion, falling
@@ -116,14 +119,15 @@ typedef struct tc_tuning {
     int32_t heavy_bitmap;   /* 0 or 1 */
     int32_t blocks_per_sm;  /* persistent grid = SMs * this (0: occupancy) */
     int32_t hash_pairs;     /* 0 or 1: bucketed-pair hash tables instead of cuckoo / linear */
-    int32_t flat_max_deg;   /* 0, 4 or 8: a graph with no row longer than this counts in one kernel */
+    int32_t flat_max_deg;   /* 0..8: a graph with no row longer than this counts in one kernel */
 } tc_tuning;
 TC_API int tc_ctx_get_tuning(tc_ctx *ctx, tc_tuning *out);
 TC_API int tc_ctx_set_tuning(tc_ctx *ctx, const tc_tuning *in);
 /* Autotuner: times the count of g under candidate thresholds (coordinate
  * descent from the current tuning over warp_max_deg, light_max_work,
- * unit_work, long_list; each candidate the median of `reps` counts) and sets
- * the fastest on ctx.  best / best_ms may be NULL.  At most max_trials
+ * unit_work, long_list, probe_kicks, heavy_bitmap, hash_pairs and
+ * flat_max_deg; each candidate the median of `reps` counts; a change is kept
+ * only if it is at least 2% faster) and sets the fastest on ctx.  best / best_ms may be NULL.  At most max_trials
  * candidates are timed. */
 TC_API int tc_autotune(tc_ctx *ctx, tc_graph *g, int max_trials, int reps, tc_tuning *best, float *best_ms);
 
