@@ -61,3 +61,32 @@ def test_rmat23_halo_parts_sum_to_whole(ctx, full):
         b.free()
         for p in parts:
             p.free()
+
+
+def test_host_csr_counts_and_rejects_at_full_size(ctx, full):
+    """tc_count_csr_i32 on a full-size host CSR (upload, validation, count,
+    read-back): the golden count, twice; an id out of range, a row out of
+    order and a non-monotone row_ptr are rejected with TC_E_FORMAT, and the
+    context stays usable."""
+    want = full["rmat21"]["triangles"]
+    rp, col = ctx.graph_from_edges(*gen.rmat(21, 16)).download()
+    assert ctx.count_csr(rp, col) == want
+    assert ctx.count_csr(rp, col) == want
+    bad_id = col.copy()
+    bad_id[len(col) // 2] = len(rp) + 5  # an id out of range in a middle stage
+    bad_order = col.copy()
+    r = int(np.searchsorted(rp, 7 * len(col) // 8))  # a row with two entries late in the array
+    while rp[r + 1] - rp[r] < 2:
+        r += 1
+    bad_order[rp[r]], bad_order[rp[r] + 1] = bad_order[rp[r] + 1], bad_order[rp[r]]
+    bad_rp = rp.copy()
+    bad_rp[len(rp) // 3] = bad_rp[len(rp) // 3 + 1] + 5  # row_ptr not monotone
+    for r_, c_ in ((rp, bad_id), (rp, bad_order), (bad_rp, col)):
+        with pytest.raises(tc.TCError) as e:
+            ctx.count_csr(r_, c_)
+        assert e.value.code == "TC_E_FORMAT"
+    assert ctx.count_csr(rp, col) == want
+    g = ctx.graph_from_edges(*gen.road(1600))  # > 4 M entries, rows <= 8: the flat count from host arrays
+    rp2, col2 = g.download()
+    assert len(col2) >= (1 << 22)
+    assert ctx.count_csr(rp2, col2) == ctx.count(g)
