@@ -342,7 +342,8 @@ def run_ours(args, world, rank, local, pg):
                          "kernel": "flat_kernel" if flat else "count_kernel", "kernel_ms": kernel_avg_ms,
                          "algorithmic_bytes_per_launch": B_alg,
                          "algorithmic_bytes_definition": "4(V+1) + 12|E+| + 4 W+ + 8, W+ = sum over oriented "
-                                                         "edges of d+(v) (SURVEY.md 8d)",
+                                                         "edges of d+(v): each root's row_ptr and list once, "
+                                                         "each oriented edge's row_ptr pair and N+(v)",
                          "probes_done": probes,
                          "achieved_min_side": (4 * (V + 1) + 12 * E + 4 * probes + 8) / (kernel_avg_ms / 1000.0) / 1e9,
                          "min_side_note": ("the flat kernel probes every wedge: its bytes are B itself" if flat else
