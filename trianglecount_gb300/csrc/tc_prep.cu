@@ -142,23 +142,119 @@ __global__ void narrow_i64_kernel(const int64_t *in, int32_t *out, int64_t n, in
     }
 }
 
-__global__ void orient_flags_kernel(const int32_t *rowid, const int32_t *col, const int32_t *deg, int64_t nnz, int tie,
-                                    uint8_t *flags) {
-    GRID_STRIDE(j, nnz) {
-        const int u = rowid[j], w = col[j];
-        flags[j] = (uint8_t)keep_edge(deg[u], deg[w], u, w, tie);
+// Orientation in two balanced passes over tiles of 4096 undirected entries
+// (256 threads x 16 contiguous entries, no per-entry flags or positions kept):
+// pass 1 decides every entry (16 keep bits per thread, kept for pass 2) and
+// counts each tile's kept entries; after a scan of the tile counts, pass 2
+// ranks the bits with one block scan and writes
+// the kept entries in order, plus every row's start (the rows that begin at
+// an entry are those between its predecessor's row and its own).
+constexpr int kOT = 256, kOI = 16, kOTile = kOT * kOI;
+
+// Exclusive scan of one value per thread over a 256-thread block; *total gets
+// the block's sum.
+__device__ __forceinline__ int block_scan_256(int v, int *total) {
+    __shared__ int wsum[kOT / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += t;
     }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < kOT / 32 ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < kOT / 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFull, w, o);
+            if (lane >= o) w += t;
+        }
+        if (lane < kOT / 32) wsum[lane] = w;
+    }
+    __syncthreads();
+    const int excl = x - v + (warp ? wsum[warp - 1] : 0);
+    *total = wsum[kOT / 32 - 1];
+    __syncthreads();  // wsum is reused by the next call
+    return excl;
 }
 
-__global__ void compact_i32_kernel(const int32_t *in, const uint8_t *flags, const int32_t *pos, int64_t n,
-                                   int32_t *out) {
-    GRID_STRIDE(j, n) {
-        if (flags[j]) out[pos[j]] = in[j];
+// Keep bits of the thread's 16 entries [j0, j0 + 16), their rows u[] and ids w[].
+__device__ __forceinline__ unsigned orient_keep16(const int32_t *__restrict__ rowid, const int32_t *__restrict__ col,
+                                                  const int32_t *__restrict__ deg, int64_t j0, int64_t nnz, int tie,
+                                                  int (&u)[kOI], int (&w)[kOI]) {
+    if (j0 + kOI <= nnz) {  // 64-byte aligned: four 16-byte loads per array
+#pragma unroll
+        for (int q = 0; q < kOI / 4; ++q) {
+            const int4 a = __ldg(reinterpret_cast<const int4 *>(rowid + j0) + q);
+            const int4 b = __ldg(reinterpret_cast<const int4 *>(col + j0) + q);
+            u[4 * q] = a.x, u[4 * q + 1] = a.y, u[4 * q + 2] = a.z, u[4 * q + 3] = a.w;
+            w[4 * q] = b.x, w[4 * q + 1] = b.y, w[4 * q + 2] = b.z, w[4 * q + 3] = b.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < kOI; ++i) {
+            const bool in = j0 + i < nnz;
+            u[i] = in ? __ldg(rowid + j0 + i) : 0;
+            w[i] = in ? __ldg(col + j0 + i) : 0;
+        }
     }
+    unsigned bits = 0;
+#pragma unroll
+    for (int i = 0; i < kOI; ++i)
+        if (j0 + i < nnz && keep_edge(__ldg(deg + u[i]), __ldg(deg + w[i]), u[i], w[i], tie)) bits |= 1u << i;
+    return bits;
 }
 
-__global__ void gather_rp_kernel(const int32_t *rp, const int32_t *pos, int64_t n_rows_plus1, int32_t *out_rp) {
-    GRID_STRIDE(u, n_rows_plus1) out_rp[u] = pos[rp[u]];
+__global__ void __launch_bounds__(kOT) orient_tile_count_kernel(const int32_t *rowid, const int32_t *col,
+                                                                 const int32_t *deg, int64_t nnz, int tie,
+                                                                 int32_t *tile_cnt, uint16_t *keep) {
+    int u[kOI], w[kOI];
+    const int64_t j0 = (int64_t)blockIdx.x * kOTile + (int64_t)threadIdx.x * kOI;
+    const unsigned bits = orient_keep16(rowid, col, deg, j0, nnz, tie, u, w);
+    keep[(int64_t)blockIdx.x * kOT + threadIdx.x] = (uint16_t)bits;  // pass 2 reads the bits back
+    int total = 0;
+    block_scan_256(__popc(bits), &total);
+    if (threadIdx.x == 0) tile_cnt[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kOT) orient_tile_write_kernel(const int32_t *__restrict__ rowid,
+                                                                 const int32_t *__restrict__ col, const uint16_t *keep,
+                                                                 int64_t nnz, int64_t V, const int32_t *tile_off,
+                                                                 int32_t *out_rp, int32_t *out_col) {
+    int u[kOI], w[kOI];
+    const int64_t j0 = (int64_t)blockIdx.x * kOTile + (int64_t)threadIdx.x * kOI;
+    const unsigned bits = keep[(int64_t)blockIdx.x * kOT + threadIdx.x];
+    if (j0 + kOI <= nnz) {
+#pragma unroll
+        for (int q = 0; q < kOI / 4; ++q) {
+            const int4 a = __ldg(reinterpret_cast<const int4 *>(rowid + j0) + q);
+            const int4 b = __ldg(reinterpret_cast<const int4 *>(col + j0) + q);
+            u[4 * q] = a.x, u[4 * q + 1] = a.y, u[4 * q + 2] = a.z, u[4 * q + 3] = a.w;
+            w[4 * q] = b.x, w[4 * q + 1] = b.y, w[4 * q + 2] = b.z, w[4 * q + 3] = b.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < kOI; ++i) {
+            const bool in = j0 + i < nnz;
+            u[i] = in ? __ldg(rowid + j0 + i) : 0;
+            w[i] = in ? __ldg(col + j0 + i) : 0;
+        }
+    }
+    int total = 0;
+    int o = tile_off[blockIdx.x] + block_scan_256(__popc(bits), &total);
+    if (j0 >= nnz) return;
+    int prev = j0 == 0 ? -1 : __ldg(rowid + j0 - 1);
+#pragma unroll
+    for (int i = 0; i < kOI; ++i) {
+        if (j0 + i >= nnz) break;
+        for (int r = prev + 1; r <= u[i]; ++r) out_rp[r] = o;  // rows that start at this entry
+        prev = u[i];
+        if ((bits >> i) & 1u) out_col[o++] = w[i];
+    }
+    if (j0 + kOI >= nnz)  // the last entry's thread: the rows after it (and out_rp[V]) start at the end
+        for (int64_t r = (int64_t)prev + 1; r <= V; ++r) out_rp[r] = o;
 }
 
 // ---- halo ----------------------------------------------------------------------
@@ -499,25 +595,29 @@ int tc_orient(tc_ctx *ctx, const tc_ugraph *ug, int tie, tc_graph **out) {
     *out = nullptr;
     cudaStream_t s = ctx->stream;
     const int64_t V = ug->n_rows, nnz = ug->nnz;
-    DBuf<uint8_t> flags;
-    DBuf<int32_t> pos, orp, ocol;
-    TC_TRY(flags.alloc((size_t)nnz, s));
-    TC_TRY(pos.alloc((size_t)nnz + 1, s));
-    if (nnz) {
-        orient_flags_kernel<<<grid(nnz, ctx), 256, 0, s>>>(ug->rowid, ug->col, ug->deg, nnz, tie, flags.p);
-        TC_CUDA(cudaGetLastError());
-    }
-    TC_TRY(scan_flags_u8(flags.p, pos.p, nnz, s));
-    int32_t m32 = 0;
-    TC_TRY(d2h_scalar(&m32, pos.p + nnz, s));
+    const int64_t tiles = (nnz + kOTile - 1) / kOTile;
+    DBuf<int32_t> tile_cnt, tile_off, orp, ocol;
+    DBuf<uint16_t> keep;
+    TC_TRY(keep.alloc((size_t)std::max<int64_t>(tiles, 1) * kOT, s));
+    TC_TRY(tile_cnt.alloc((size_t)std::max<int64_t>(tiles, 1), s));
+    TC_TRY(tile_off.alloc((size_t)tiles + 1, s));
     TC_TRY(orp.alloc((size_t)V + 1, s));
-    TC_TRY(ocol.alloc((size_t)std::max<int32_t>(m32, 1), s));
-    if (nnz) {
-        compact_i32_kernel<<<grid(nnz, ctx), 256, 0, s>>>(ug->col, flags.p, pos.p, nnz, ocol.p);
+    int32_t m32 = 0;
+    if (tiles) {
+        orient_tile_count_kernel<<<(unsigned)tiles, kOT, 0, s>>>(ug->rowid, ug->col, ug->deg, nnz, tie, tile_cnt.p,
+                                                                  keep.p);
         TC_CUDA(cudaGetLastError());
+        TC_TRY(scan_exclusive_i32(tile_cnt.p, tile_off.p, tiles, s));  // tile_off[tiles] = the kept total
+        TC_TRY(d2h_scalar(&m32, tile_off.p + tiles, s));
     }
-    gather_rp_kernel<<<grid(V + 1, ctx), 256, 0, s>>>(ug->rp, pos.p, V + 1, orp.p);
-    TC_CUDA(cudaGetLastError());
+    TC_TRY(ocol.alloc((size_t)std::max<int32_t>(m32, 1), s));
+    if (tiles) {
+        orient_tile_write_kernel<<<(unsigned)tiles, kOT, 0, s>>>(ug->rowid, ug->col, keep.p, nnz, V, tile_off.p,
+                                                                  orp.p, ocol.p);
+        TC_CUDA(cudaGetLastError());
+    } else {
+        TC_CUDA(cudaMemsetAsync(orp.p, 0, sizeof(int32_t) * (size_t)(V + 1), s));
+    }
     TC_CUDA(cudaStreamSynchronize(s));
     tc_graph *g = nullptr;
     TC_TRY(graph_adopt_device(ctx, orp.p, ocol.p, V, m32, V, &g));
