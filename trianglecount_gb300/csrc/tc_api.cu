@@ -51,17 +51,32 @@ __global__ void max_row_kernel(const int32_t *rp, int64_t n_rows, int *out) {
     if ((threadIdx.x & 31) == 0 && longest) atomicMax(out, longest);
 }
 
+// Four entries per thread: one 16-byte load of col[j..j+4), the next entry
+// and the four row-start marks after them (col is 256-byte aligned).
 __global__ void check_cols_kernel(const int32_t *col, int64_t nnz, int64_t n_rows, const uint8_t *start,
                                   ValidateErr *err) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nnz; j += stride) {
-        const int x = col[j];
-        int code = 0;
-        if (x < 0 || x >= n_rows) code = 2;
-        else if (j + 1 < nnz && !start[j + 1] && col[j + 1] <= x) code = 3;
-        if (code) {
-            atomicMax(&err->code, code);
-            atomicMin(&err->first, (int)j);
+    const int64_t groups = (nnz + 3) / 4;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < groups; q += stride) {
+        const int64_t j0 = 4 * q;
+        int x[5];
+        if (j0 + 4 <= nnz) {
+            const int4 v = __ldg(reinterpret_cast<const int4 *>(col) + q);
+            x[0] = v.x, x[1] = v.y, x[2] = v.z, x[3] = v.w;
+        } else {
+            for (int i = 0; i < 4; ++i) x[i] = j0 + i < nnz ? __ldg(col + j0 + i) : 0;
+        }
+        x[4] = j0 + 4 < nnz ? __ldg(col + j0 + 4) : 0;
+        for (int i = 0; i < 4; ++i) {
+            const int64_t j = j0 + i;
+            if (j >= nnz) break;
+            int code = 0;
+            if (x[i] < 0 || x[i] >= n_rows) code = 2;
+            else if (j + 1 < nnz && !__ldg(start + j + 1) && x[i + 1] <= x[i]) code = 3;
+            if (code) {
+                atomicMax(&err->code, code);
+                atomicMin(&err->first, (int)j);
+            }
         }
     }
 }
