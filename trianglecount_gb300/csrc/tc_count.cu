@@ -150,10 +150,12 @@ __device__ __forceinline__ uint32_t cuckoo_probe(const int *tab, int shift, int 
 // passes is flagged (bit 31 of the bucket's first slot, which is occupied), so
 // a lookup reads past a bucket only when that bucket is flagged.  At a load of
 // at most 1/4 (half a key per bucket on average) about 1.4% of the buckets
-// hold more than two home keys, so nearly every probe is one shared load --
-// against two for the cuckoo hash -- and random 8-byte loads conflict less per
-// key than two random 4-byte loads.  Keys are vertex ids <= 2^31 - 2, so a
-// flagged slot (key | 2^31, negative, not -1) never reads as empty or as a key.
+// hold more than two home keys, so nearly every probe is one shared load
+// against two for the cuckoo hash.  Measured slower than the cuckoo hash all
+// the same (the wider loads and the rare flagged chains cost more than the
+// second load saves), so it is an autotuner candidate only.  Keys are vertex
+// ids <= 2^31 - 2, so a flagged slot (key | 2^31, negative, not -1) never
+// reads as empty or as a key.
 constexpr int kFlagBit = (int)0x80000000u;
 constexpr int kKeyBits = 0x7fffffff;
 
@@ -210,7 +212,7 @@ __device__ __forceinline__ uint32_t probe_any(const int *tab, uint32_t mask, int
 }
 
 // Fills an emptied table with the keys keys[i], i in [tid, n) step nthreads, in
-// the preferred mode; returns the mode the table ended in, or -1 when a cuckoo
+// the preferred mode and returns that mode; *ok turns false when a cuckoo
 // insertion gave up (the caller then empties the table and inserts linearly).
 template <bool kPairsOnly>
 __device__ __forceinline__ int table_fill(int *tab, uint32_t mask, int shift, const int32_t *__restrict__ keys, int n,
@@ -517,8 +519,8 @@ __global__ void __launch_bounds__(kThreads) split_in_count_kernel(const unsigned
 }
 
 // transpose + classify: scatter the chunk's middle-centric edges into the
-// in-lists, then classify each row of the chunk as a light task, a heavy task
-// (block units) or no work.
+// in-lists, then classify each row of the chunk as a micro task (mask), a
+// light task (list), a heavy task (block units) or no work.
 __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P, HeavyEntry *heavy) {
     const int lane = threadIdx.x & (kWarp - 1);
     // Block-unit size: unit_work, or less on a small job so that every count
