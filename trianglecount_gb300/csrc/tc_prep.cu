@@ -5,8 +5,10 @@
 // (remove_self_loop, to_bidirected, remove isolated nodes, adj_tensors('csr')):
 //   keys (u<<B|v) and (v<<B|u) per non-loop edge -> LSD radix sort -> unique
 //   -> per-vertex counts -> order-preserving relabel of non-isolated vertices.
-// Orientation restates Find_size / cp.cumsum / Convert (:19-111, :253-270):
-//   keep flag per entry -> exclusive scan -> stable scatter, so rows stay ascending.
+// Orientation restates Find_size / cp.cumsum / Convert (:19-111, :253-270)
+// (count the kept entries, scan, write them in order), over 4096-entry tiles:
+//   keep bits + tile counts -> scan of the tile counts -> ordered write of the
+//   kept entries and the new row starts, so rows stay ascending.
 // Halo extraction restates create_subgraph_with_halo
 // (preprocess_GPU/Halo_cleanned_preprocess/round_clean_subgraph.cu:357-902) with the
 // intended prune loop of Halo_creation_preprocess.py:566-589: halo vertices with
