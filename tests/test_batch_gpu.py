@@ -32,3 +32,26 @@ def test_batch_async_and_single(ctx):
     assert list(b.results()) == [t]
     # the same graph several times in one batch
     assert list(ctx.batch([g, g, g]).run()) == [t, t, t]
+
+
+def test_batch_mixes_degenerate_and_bounded_degree_graphs(ctx):
+    """One batch holding an empty graph, an edgeless one, a single triangle, a
+    halo-style graph (roots a prefix of the rows), a road grid (counted by the
+    flat kernel on its own, by the chain inside a batch) and R-MAT graphs:
+    every per-graph result equals its own plain count and the oracle."""
+    cases = [(np.zeros(1, np.int32), np.zeros(0, np.int32), None),
+             (np.zeros(7, np.int32), np.zeros(0, np.int32), None),
+             (np.array([0, 2, 3, 3], np.int32), np.array([1, 2, 2], np.int32), None)]
+    rp, col, _ = oracle.pipeline(*gen.rmat(11))
+    cases.append((rp, col, len(rp) // 3))
+    for src, dst in (gen.road(120), gen.rmat(12), gen.rmat(9)):
+        rp, col, _ = oracle.pipeline(src, dst)
+        cases.append((rp, col, None))
+    graphs = [ctx.upload(rp, col, n_roots=nr) for rp, col, nr in cases]
+    want = [oracle.count(rp, col, n_roots=nr) if nr is not None else oracle.count(rp, col)
+            for rp, col, nr in cases]
+    assert list(ctx.count_each(graphs)) == want
+    b = ctx.batch(graphs)
+    for _ in range(2):
+        assert list(b.run()) == want
+    b.free()
