@@ -298,7 +298,7 @@ int graph_rebind(tc_graph *g, tc_ctx *ctx) {
 
 size_t graph_device_bytes(const tc_graph *g) {
     const size_t csr = sizeof(int32_t) * (size_t)(g->n_rows + 1 + g->nnz);
-    const size_t scratch = (size_t)(g->n_rows + 1) * (4 + 4 + 8 + 8 + 16 + 1) + (size_t)g->nnz * 5 + 1024;
+    const size_t scratch = (size_t)(g->n_rows + 1) * (4 + 4 + 8 + 8 + 4 + 16 + 1) + (size_t)g->nnz * 5 + 1024;
     return csr + scratch;
 }
 
