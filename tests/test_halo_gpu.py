@@ -45,3 +45,28 @@ def test_halo_with_empty_part(ctx):
     parts = ctx.halo_extract(ug, part, 3)
     assert parts[1].n_rows == 0 and parts[2].n_rows == 0
     assert ctx.count(parts[0]) == oracle.count(*oracle.orient(rp, col))
+
+
+@pytest.mark.parametrize("n", [1024, 2048, 1023])
+@pytest.mark.parametrize("k", [1, 3])
+def test_halo_tile_boundaries(ctx, n, k):
+    """Circulant graphs C_n(1, 2): 4n undirected entries, so n = 1024 and 2048
+    fill exactly one and two 4096-entry tiles (the last row ends on a tile
+    boundary) and n = 1023 stops four entries short of one."""
+    i = np.arange(n, dtype=np.int64)
+    src = np.concatenate([i, i])
+    dst = np.concatenate([(i + 1) % n, (i + 2) % n])
+    rp, col = oracle.clean(src, dst)
+    assert len(col) == 4 * n
+    deg = np.diff(rp)
+    part = gen.parts_random(n, k)
+    ug = ctx.upload_ugraph(rp, col, deg)
+    parts = ctx.halo_extract(ug, part, k)
+    total = 0
+    for p, g in enumerate(parts):
+        lrp, lcol, t_ver = oracle.halo_part(rp, col, deg, part, p)
+        drp, dcol = g.download()
+        assert g.n_roots == t_ver
+        assert np.array_equal(drp, lrp) and np.array_equal(dcol, lcol), (n, k, p)
+        total += ctx.count(g)
+    assert total == oracle.count(*oracle.orient(rp, col)) == n

@@ -11,8 +11,11 @@
 //   kept entries and the new row starts, so rows stay ascending.
 // Halo extraction restates create_subgraph_with_halo
 // (preprocess_GPU/Halo_cleanned_preprocess/round_clean_subgraph.cu:357-902) with the
-// intended prune loop of Halo_creation_preprocess.py:566-589: halo vertices with
-// zero in-degree are peeled until none is left.
+// intended prune loop of Halo_creation_preprocess.py:566-589: per part, local
+// ids (part vertices, then halo, each ascending) -> P/H class bits, tile counts,
+// row-start ranks and halo in-degrees over the orientation's tiles -> scan ->
+// local row lengths -> scan -> ordered write of every local edge; then halo
+// vertices with zero in-degree are peeled until none is left.
 #include <algorithm>
 #include <vector>
 
@@ -182,10 +185,9 @@ __device__ __forceinline__ int block_scan_256(int v, int *total) {
     return excl;
 }
 
-// Keep bits of the thread's 16 entries [j0, j0 + 16), their rows u[] and ids w[].
-__device__ __forceinline__ unsigned orient_keep16(const int32_t *__restrict__ rowid, const int32_t *__restrict__ col,
-                                                  const int32_t *__restrict__ deg, int64_t j0, int64_t nnz, int tie,
-                                                  int (&u)[kOI], int (&w)[kOI]) {
+// The thread's 16 entries [j0, j0 + 16): rows u[] and ids w[] (0 past nnz).
+__device__ __forceinline__ void load16(const int32_t *__restrict__ rowid, const int32_t *__restrict__ col, int64_t j0,
+                                       int64_t nnz, int (&u)[kOI], int (&w)[kOI]) {
     if (j0 + kOI <= nnz) {  // 64-byte aligned: four 16-byte loads per array
 #pragma unroll
         for (int q = 0; q < kOI / 4; ++q) {
@@ -202,6 +204,13 @@ __device__ __forceinline__ unsigned orient_keep16(const int32_t *__restrict__ ro
             w[i] = in ? __ldg(col + j0 + i) : 0;
         }
     }
+}
+
+// Keep bits of the thread's 16 entries [j0, j0 + 16), their rows u[] and ids w[].
+__device__ __forceinline__ unsigned orient_keep16(const int32_t *__restrict__ rowid, const int32_t *__restrict__ col,
+                                                  const int32_t *__restrict__ deg, int64_t j0, int64_t nnz, int tie,
+                                                  int (&u)[kOI], int (&w)[kOI]) {
+    load16(rowid, col, j0, nnz, u, w);
     unsigned bits = 0;
 #pragma unroll
     for (int i = 0; i < kOI; ++i)
@@ -228,22 +237,7 @@ __global__ void __launch_bounds__(kOT) orient_tile_write_kernel(const int32_t *_
     int u[kOI], w[kOI];
     const int64_t j0 = (int64_t)blockIdx.x * kOTile + (int64_t)threadIdx.x * kOI;
     const unsigned bits = keep[(int64_t)blockIdx.x * kOT + threadIdx.x];
-    if (j0 + kOI <= nnz) {
-#pragma unroll
-        for (int q = 0; q < kOI / 4; ++q) {
-            const int4 a = __ldg(reinterpret_cast<const int4 *>(rowid + j0) + q);
-            const int4 b = __ldg(reinterpret_cast<const int4 *>(col + j0) + q);
-            u[4 * q] = a.x, u[4 * q + 1] = a.y, u[4 * q + 2] = a.z, u[4 * q + 3] = a.w;
-            w[4 * q] = b.x, w[4 * q + 1] = b.y, w[4 * q + 2] = b.z, w[4 * q + 3] = b.w;
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < kOI; ++i) {
-            const bool in = j0 + i < nnz;
-            u[i] = in ? __ldg(rowid + j0 + i) : 0;
-            w[i] = in ? __ldg(col + j0 + i) : 0;
-        }
-    }
+    load16(rowid, col, j0, nnz, u, w);
     int total = 0;
     int o = tile_off[blockIdx.x] + block_scan_256(__popc(bits), &total);
     if (j0 >= nnz) return;
@@ -277,50 +271,144 @@ __global__ void local_ids_kernel(const uint8_t *inP, const uint8_t *inH, const i
     GRID_STRIDE(v, n) lid[v] = inP[v] ? lidP[v] : (inH[v] ? t_ver + lidH[v] : -1);
 }
 
-// flagsP/flagsH: entry j of a combined source is an oriented edge to a part
-// (P) or halo (H) vertex of the combined set.  cnt[lid(src)] counts both.
-__global__ void halo_edge_flags_kernel(const int32_t *rowid, const int32_t *col, const int32_t *deg, int64_t nnz,
-                                       const int32_t *lid, const uint8_t *inP, int tie, uint8_t *fP, uint8_t *fH,
-                                       int32_t *cnt) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const int64_t start = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t rounds = (nnz + stride - 1) / stride;
-    for (int64_t r = 0; r < rounds; ++r) {
-        const int64_t j = start + r * stride;
-        bool keep = false;
-        int ls = 0;
-        if (j < nnz) {
-            const int s = rowid[j], d = col[j];
-            ls = lid[s];
-            const int ld = lid[d];
-            keep = ls >= 0 && ld >= 0 && keep_edge(deg[s], deg[d], s, d, tie);
-            const bool toP = keep && inP[d];
-            fP[j] = (uint8_t)toP;
-            fH[j] = (uint8_t)(keep && !toP);
+// Local edges over the orientation's 4096-entry tiles.  Entry j (row s, id d)
+// is a local edge of the part when both ends have a local id and s -> d is the
+// oriented direction: a P entry when d is a part vertex (local id < t_ver),
+// else an H entry.  A local row lists its P entries, then its H entries, each
+// in the undirected row's (ascending) order, so an entry's offset in its local
+// row is its rank among the row's entries of its class (plus the row's P count
+// for an H entry).  Ranks come from the tiles' P and H counts, scanned, and one
+// block scan per tile, as in the orientation; no per-entry flag or position
+// array is written.
+//
+// Pass 1 stores the 32 class bits of each thread's 16 entries (P in the low
+// half, H in the high half), the tile's P and H counts (tile_cnt[t] and
+// tile_cnt[tiles + t]) and every row's P and H ranks within the tile of its
+// start (packed 16 + 16 bits: a tile holds 4096 entries), and counts each halo
+// vertex's in-degree (its H entries) for the prune.
+__global__ void __launch_bounds__(kOT) halo_tile_count_kernel(const int32_t *__restrict__ rowid,
+                                                               const int32_t *__restrict__ col,
+                                                               const int32_t *__restrict__ deg,
+                                                               const int32_t *__restrict__ lid, int64_t nnz, int64_t V,
+                                                               int64_t tiles, int t_ver, int tie,
+                                                               uint32_t *__restrict__ bits,
+                                                               int32_t *__restrict__ tile_cnt,
+                                                               uint32_t *__restrict__ row_rank,
+                                                               int32_t *__restrict__ indeg) {
+    int u[kOI], w[kOI];
+    const int64_t j0 = (int64_t)blockIdx.x * kOTile + (int64_t)threadIdx.x * kOI;
+    load16(rowid, col, j0, nnz, u, w);
+    unsigned pb = 0, hb = 0;
+    int cs = -1, cls = -1, cdeg = 0;  // the current row: id, local id, degree
+#pragma unroll
+    for (int i = 0; i < kOI; ++i) {
+        if (j0 + i >= nnz) break;
+        if (u[i] != cs) {
+            cs = u[i];
+            cls = __ldg(lid + cs);
+            cdeg = __ldg(deg + cs);
         }
-        warp_count(cnt, ls, keep);
+        if (cls < 0) continue;
+        const int ld = __ldg(lid + w[i]);
+        if (ld < 0 || !keep_edge(cdeg, __ldg(deg + w[i]), cs, w[i], tie)) continue;
+        if (ld < t_ver) {
+            pb |= 1u << i;
+        } else {
+            hb |= 1u << i;
+            atomicAdd(indeg + ld, 1);
+        }
+    }
+    bits[(int64_t)blockIdx.x * kOT + threadIdx.x] = pb | (hb << 16);
+    int total = 0;
+    const int excl = block_scan_256((int)(__popc(pb) | (__popc(hb) << 16)), &total);
+    if (threadIdx.x == 0) {
+        tile_cnt[blockIdx.x] = total & 0xffff;
+        tile_cnt[tiles + blockIdx.x] = total >> 16;
+    }
+    if (j0 >= nnz) return;
+    int prev = j0 == 0 ? -1 : __ldg(rowid + j0 - 1);
+#pragma unroll
+    for (int i = 0; i < kOI; ++i) {
+        if (j0 + i >= nnz) break;
+        if (u[i] == prev) continue;
+        const unsigned below = (1u << i) - 1u;
+        const uint32_t rk = (uint32_t)excl + (__popc(pb & below) | (__popc(hb & below) << 16));
+        for (int r = prev + 1; r <= u[i]; ++r) row_rank[r] = rk;  // rows that start at this entry
+        prev = u[i];
+    }
+    if (j0 + kOI >= nnz) {  // the last entry's thread: the rows after it (and row V) start at the end
+        const uint32_t rk = (uint32_t)excl + (__popc(pb) | (__popc(hb) << 16));
+        for (int64_t r = (int64_t)prev + 1; r <= V; ++r) row_rank[r] = rk;
     }
 }
 
-__global__ void halo_scatter_kernel(const int32_t *rowid, const int32_t *col, const int32_t *rp, int64_t nnz,
-                                    const int32_t *lid, const uint8_t *fP, const uint8_t *fH, const int32_t *posP,
-                                    const int32_t *posH, const int32_t *lrp, int32_t *lcol, int32_t *lrow) {
-    GRID_STRIDE(j, nnz) {
-        if (!fP[j] && !fH[j]) continue;
-        const int s = rowid[j];
-        const int a = rp[s], b = rp[s + 1];
-        const int ls = lid[s];
-        int off;
-        if (fP[j]) off = posP[j] - posP[a];
-        else off = (posP[b] - posP[a]) + (posH[j] - posH[a]);
-        const int o = lrp[ls] + off;
-        lcol[o] = lid[col[j]];
+// Global P and H ranks of entry index a, whose row-start rank (within the tile
+// of a; the last tile for a = nnz) is rk.  off[] is the exclusive scan of the
+// 2 * tiles tile counts.
+__device__ __forceinline__ void halo_rank(int a, uint32_t rk, const int32_t *off, int64_t tiles, int &pr, int &hr) {
+    const int64_t t = min((int64_t)(a / kOTile), tiles - 1);
+    pr = off[t] + (int)(rk & 0xffffu);
+    hr = off[tiles + t] - off[tiles] + (int)(rk >> 16);
+}
+
+// Per vertex of the part's combined set: its P and H entry counts (from the
+// ranks at its row's start and at the next row's start) -> cnt[local id], and
+// the bases that turn an entry's global rank into its local-row offset.
+__global__ void halo_rows_kernel(const int32_t *__restrict__ rp, const int32_t *__restrict__ lid,
+                                 const uint32_t *__restrict__ row_rank, const int32_t *__restrict__ off, int64_t V,
+                                 int64_t tiles, int32_t *__restrict__ cnt, int32_t *__restrict__ base_p,
+                                 int32_t *__restrict__ base_h) {
+    GRID_STRIDE(v, V) {
+        const int l = lid[v];
+        if (l < 0) continue;
+        int pa, ha, pb, hb;
+        halo_rank(rp[v], row_rank[v], off, tiles, pa, ha);
+        halo_rank(rp[v + 1], row_rank[v + 1], off, tiles, pb, hb);
+        const int np = pb - pa;
+        cnt[l] = np + (hb - ha);
+        base_p[v] = pa;       // P entry of rank x: local offset x - pa
+        base_h[v] = ha - np;  // H entry of rank x: local offset np + (x - ha)
+    }
+}
+
+// Pass 2: ranks each tile's P and H entries again from the stored bits and
+// writes every local edge at lrp[local row] + its offset (lcol = the local id
+// of the target, lrow = the local row, for the prune's compaction).
+__global__ void __launch_bounds__(kOT) halo_tile_write_kernel(const int32_t *__restrict__ rowid,
+                                                               const int32_t *__restrict__ col,
+                                                               const int32_t *__restrict__ lid,
+                                                               const uint32_t *__restrict__ bits, int64_t nnz,
+                                                               int64_t tiles, const int32_t *__restrict__ off,
+                                                               const int32_t *__restrict__ lrp,
+                                                               const int32_t *__restrict__ base_p,
+                                                               const int32_t *__restrict__ base_h,
+                                                               int32_t *__restrict__ lcol, int32_t *__restrict__ lrow) {
+    int u[kOI], w[kOI];
+    const int64_t j0 = (int64_t)blockIdx.x * kOTile + (int64_t)threadIdx.x * kOI;
+    const uint32_t b = bits[(int64_t)blockIdx.x * kOT + threadIdx.x];
+    const unsigned pb = b & 0xffffu, hb = b >> 16;
+    int total = 0;
+    const int excl = block_scan_256((int)(__popc(pb) | (__popc(hb) << 16)), &total);
+    if (j0 >= nnz || b == 0) return;
+    load16(rowid, col, j0, nnz, u, w);
+    int pr = off[blockIdx.x] + (excl & 0xffff);
+    int hr = off[tiles + blockIdx.x] - off[tiles] + (excl >> 16);
+    int cs = -1, ls = 0, offp = 0, offh = 0;
+#pragma unroll
+    for (int i = 0; i < kOI; ++i) {
+        const unsigned bit = 1u << i;
+        if (!(b & (bit | (bit << 16)))) continue;
+        if (u[i] != cs) {
+            cs = u[i];
+            ls = __ldg(lid + cs);
+            const int lr = __ldg(lrp + ls);
+            offp = lr - __ldg(base_p + cs);
+            offh = lr - __ldg(base_h + cs);
+        }
+        const int o = (pb & bit) ? offp + pr++ : offh + hr++;
+        lcol[o] = __ldg(lid + w[i]);
         lrow[o] = ls;
     }
-}
-
-__global__ void indeg_kernel(const int32_t *lcol, int64_t n, int32_t *indeg) {
-    GRID_STRIDE(j, n) atomicAdd(&indeg[lcol[j]], 1);
 }
 
 __global__ void frontier_init_kernel(const int32_t *indeg, int64_t n, int t_ver, uint8_t *removed, int32_t *front,
@@ -647,8 +735,10 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
     const int64_t V = ug->n_rows, nnz = ug->nnz;
     for (int64_t v = 0; v < V; ++v)
         if (part[v] < 0) return set_error(TC_E_RANGE, "part[%lld] = %d is negative", (long long)v, part[v]);
-    DBuf<int32_t> dpart, lidP, lidH, lid, cnt, lrp, posP, posH;
-    DBuf<uint8_t> inP, inH, fP, fH;
+    const int64_t tiles = (nnz + kOTile - 1) / kOTile;
+    DBuf<int32_t> dpart, lidP, lidH, lid, cnt, lrp, tile_cnt, tile_off, base_p, base_h;
+    DBuf<uint32_t> bits, row_rank;
+    DBuf<uint8_t> inP, inH;
     TC_TRY(dpart.alloc((size_t)std::max<int64_t>(V, 1), s));
     if (V) TC_CUDA(cudaMemcpyAsync(dpart.p, part, sizeof(int32_t) * (size_t)V, cudaMemcpyHostToDevice, s));
     TC_TRY(inP.alloc((size_t)V, s));
@@ -658,10 +748,12 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
     TC_TRY(lid.alloc((size_t)std::max<int64_t>(V, 1), s));
     TC_TRY(cnt.alloc((size_t)V + 1, s));
     TC_TRY(lrp.alloc((size_t)V + 1, s));
-    TC_TRY(fP.alloc((size_t)nnz, s));
-    TC_TRY(fH.alloc((size_t)nnz, s));
-    TC_TRY(posP.alloc((size_t)nnz + 1, s));
-    TC_TRY(posH.alloc((size_t)nnz + 1, s));
+    TC_TRY(base_p.alloc((size_t)std::max<int64_t>(V, 1), s));
+    TC_TRY(base_h.alloc((size_t)std::max<int64_t>(V, 1), s));
+    TC_TRY(row_rank.alloc((size_t)V + 1, s));
+    TC_TRY(bits.alloc((size_t)std::max<int64_t>(tiles, 1) * kOT, s));
+    TC_TRY(tile_cnt.alloc((size_t)std::max<int64_t>(2 * tiles, 1), s));
+    TC_TRY(tile_off.alloc((size_t)2 * tiles + 1, s));
     const int gV = grid(V, ctx), gE = grid(nnz, ctx);
     // one part; any failure returns its status (the caller frees all parts)
     auto one_part = [&](int p) -> int {
@@ -672,38 +764,46 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
         TC_TRY(scan_flags_u8(inP.p, lidP.p, V, s));
         TC_TRY(scan_flags_u8(inH.p, lidH.p, V, s));
         int32_t t_ver = 0, n_halo = 0;
-        TC_TRY(d2h_scalar(&t_ver, lidP.p + V, s));
-        TC_TRY(d2h_scalar(&n_halo, lidH.p + V, s));
+        TC_CUDA(cudaMemcpyAsync(&t_ver, lidP.p + V, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        TC_CUDA(cudaMemcpyAsync(&n_halo, lidH.p + V, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        TC_CUDA(cudaStreamSynchronize(s));
         const int64_t n_comb = (int64_t)t_ver + n_halo;
         if (V) local_ids_kernel<<<gV, 256, 0, s>>>(inP.p, inH.p, lidP.p, lidH.p, V, t_ver, lid.p);
-        TC_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * ((size_t)n_comb + 1), s));
-        if (nnz)
-            halo_edge_flags_kernel<<<gE, 256, 0, s>>>(ug->rowid, ug->col, ug->deg, nnz, lid.p, inP.p, tie, fP.p, fH.p,
-                                                      cnt.p);
-        TC_CUDA(cudaGetLastError());
+        DBuf<int32_t> indeg;
+        TC_TRY(indeg.alloc((size_t)std::max<int64_t>(n_comb, 1), s));
+        TC_CUDA(cudaMemsetAsync(indeg.p, 0, sizeof(int32_t) * (size_t)std::max<int64_t>(n_comb, 1), s));
+        if (tiles) {
+            halo_tile_count_kernel<<<(unsigned)tiles, kOT, 0, s>>>(ug->rowid, ug->col, ug->deg, lid.p, nnz, V, tiles,
+                                                                    t_ver, tie, bits.p, tile_cnt.p, row_rank.p,
+                                                                    indeg.p);
+            TC_CUDA(cudaGetLastError());
+            TC_TRY(scan_exclusive_i32(tile_cnt.p, tile_off.p, 2 * tiles, s));
+            if (V)
+                halo_rows_kernel<<<gV, 256, 0, s>>>(ug->rp, lid.p, row_rank.p, tile_off.p, V, tiles, cnt.p, base_p.p,
+                                                    base_h.p);
+            TC_CUDA(cudaGetLastError());
+        } else {
+            TC_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * ((size_t)n_comb + 1), s));
+        }
         TC_TRY(scan_exclusive_i32(cnt.p, lrp.p, n_comb, s));
-        TC_TRY(scan_flags_u8(fP.p, posP.p, nnz, s));
-        TC_TRY(scan_flags_u8(fH.p, posH.p, nnz, s));
         int32_t lnnz = 0;
         TC_TRY(d2h_scalar(&lnnz, lrp.p + n_comb, s));
-        DBuf<int32_t> lcol, lrow, indeg, front, next, fn;
+        DBuf<int32_t> lcol, lrow, front, next, fn;
         DBuf<uint8_t> removed;
         TC_TRY(lcol.alloc((size_t)lnnz, s));
         TC_TRY(lrow.alloc((size_t)lnnz, s));
-        if (nnz)
-            halo_scatter_kernel<<<gE, 256, 0, s>>>(ug->rowid, ug->col, ug->rp, nnz, lid.p, fP.p, fH.p, posP.p, posH.p,
-                                                   lrp.p, lcol.p, lrow.p);
+        if (tiles && lnnz)
+            halo_tile_write_kernel<<<(unsigned)tiles, kOT, 0, s>>>(ug->rowid, ug->col, lid.p, bits.p, nnz, tiles,
+                                                                    tile_off.p, lrp.p, base_p.p, base_h.p, lcol.p,
+                                                                    lrow.p);
         TC_CUDA(cudaGetLastError());
         // prune: peel halo vertices of zero in-degree until none is left
-        TC_TRY(indeg.alloc((size_t)std::max<int64_t>(n_comb, 1), s));
         TC_TRY(removed.alloc((size_t)std::max<int64_t>(n_comb, 1), s));
         TC_TRY(front.alloc((size_t)std::max<int32_t>(n_halo, 1), s));
         TC_TRY(next.alloc((size_t)std::max<int32_t>(n_halo, 1), s));
         TC_TRY(fn.alloc(2, s));
-        TC_CUDA(cudaMemsetAsync(indeg.p, 0, sizeof(int32_t) * (size_t)std::max<int64_t>(n_comb, 1), s));
         TC_CUDA(cudaMemsetAsync(removed.p, 0, (size_t)std::max<int64_t>(n_comb, 1), s));
         TC_CUDA(cudaMemsetAsync(fn.p, 0, 2 * sizeof(int32_t), s));
-        if (lnnz) indeg_kernel<<<grid(lnnz, ctx), 256, 0, s>>>(lcol.p, lnnz, indeg.p);
         if (n_comb) frontier_init_kernel<<<grid(n_comb, ctx), 256, 0, s>>>(indeg.p, n_comb, t_ver, removed.p, front.p, fn.p);
         TC_CUDA(cudaGetLastError());
         int32_t n_front = 0, n_removed = 0;
@@ -738,8 +838,9 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
             TC_TRY(scan_flags_u8(alive.p, nid.p, n_comb, s));
             TC_TRY(scan_exclusive_i32(len.p, newpos.p, n_comb, s));
             int32_t nl = 0, nn = 0;
-            TC_TRY(d2h_scalar(&nl, nid.p + n_comb, s));
-            TC_TRY(d2h_scalar(&nn, newpos.p + n_comb, s));
+            TC_CUDA(cudaMemcpyAsync(&nl, nid.p + n_comb, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            TC_CUDA(cudaMemcpyAsync(&nn, newpos.p + n_comb, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            TC_CUDA(cudaStreamSynchronize(s));
             n_local = nl;
             out_nnz = nn;
             TC_TRY(rp2.alloc((size_t)nl + 1, s));
