@@ -211,9 +211,11 @@ TC_API int tc_count_each(tc_ctx *ctx, tc_graph *const *graphs, int n_graphs, uin
  * hint (max id + 1 is used when larger).  Ids must be < 2^31. */
 TC_API int tc_ugraph_from_edges(tc_ctx *ctx, const int64_t *src, const int64_t *dst, int64_t n_edges,
                                 int64_t n_nodes, tc_ugraph **out);
-/* Upload an undirected CSR (e.g. a _part.csr file, Halo_creation_preprocess.py:259-278).
- * deg may be NULL (row lengths are used); otherwise it is the file's degree
- * column used by the halo orientation (round_clean_subgraph.cu:172, 178). */
+/* Upload an undirected CSR (e.g. a _part.csr file, Halo_creation_preprocess.py:259-278):
+ * rows ascending, every edge listed in both rows, no self-loop (TC_E_FORMAT /
+ * TC_E_INVALID otherwise).  deg may be NULL (row lengths are used); otherwise
+ * it is the file's degree column used by the halo orientation
+ * (round_clean_subgraph.cu:172, 178). */
 TC_API int tc_ugraph_upload_i64(tc_ctx *ctx, const int64_t *row_ptr, const int64_t *col, const int64_t *deg,
                                 int64_t n_rows, int64_t nnz, tc_ugraph **out);
 TC_API int tc_ugraph_info(const tc_ugraph *g, int64_t *n_rows, int64_t *nnz);

@@ -70,3 +70,22 @@ def test_halo_tile_boundaries(ctx, n, k):
         assert np.array_equal(drp, lrp) and np.array_equal(dcol, lcol), (n, k, p)
         total += ctx.count(g)
     assert total == oracle.count(*oracle.orient(rp, col)) == n
+
+
+@pytest.mark.parametrize("k, n_labels", [(40, 40), (3, 5), (3, 36)])
+def test_halo_many_parts_and_unassigned_vertices(ctx, k, n_labels):
+    """k > 32 takes the per-part halo pass instead of the all-parts masks;
+    labels >= k (also >= 32) put vertices in no extracted part, though they
+    can still be in a part's halo."""
+    src, dst = gen.rmat(12)
+    rp, col = oracle.clean(src, dst)
+    deg = np.diff(rp)
+    part = np.random.default_rng(k * 100 + n_labels).integers(0, n_labels, len(rp) - 1).astype(np.int32)
+    ug = ctx.upload_ugraph(rp, col, deg)
+    parts = ctx.halo_extract(ug, part, k)
+    assert len(parts) == k
+    for p, g in enumerate(parts):
+        lrp, lcol, t_ver = oracle.halo_part(rp, col, deg, part, p)
+        drp, dcol = g.download()
+        assert g.n_roots == t_ver
+        assert np.array_equal(drp, lrp) and np.array_equal(dcol, lcol), (k, n_labels, p)

@@ -56,3 +56,17 @@ def test_upload_ugraph_roundtrip(ctx):
     ug = ctx.upload_ugraph(rp, col, deg)
     r2, c2, d2 = ug.download()
     assert np.array_equal(r2, rp) and np.array_equal(c2, col) and np.array_equal(d2, deg)
+
+
+def test_upload_ugraph_rejects_asymmetric_and_self_loops(ctx):
+    """An undirected CSR lists every edge in both rows and has no self-loop;
+    the halo extraction reads each edge from either end."""
+    import trianglecount_gb300 as tc
+    missing = (np.array([0, 2, 3, 3], np.int64), np.array([1, 2, 0], np.int64))  # 0-2 absent from row 2
+    loop = (np.array([0, 2, 3, 5], np.int64), np.array([1, 2, 0, 0, 2], np.int64))  # self-loop 2-2
+    for rp, col in (missing, loop):
+        with pytest.raises(tc.TCError) as e:
+            ctx.upload_ugraph(rp, col)
+        assert e.value.code == "TC_E_INVALID"
+    ug = ctx.upload_ugraph(np.array([0, 2, 3, 4], np.int64), np.array([1, 2, 0, 0], np.int64))  # 0-1, 0-2
+    assert ug.info() == (3, 4)

@@ -130,6 +130,23 @@ __global__ void degree_kernel(const int32_t *rp, int64_t n, int32_t *deg) {
     GRID_STRIDE(v, n) deg[v] = rp[v + 1] - rp[v];
 }
 
+// An undirected CSR lists every edge in both rows and has no self-loop: entry
+// (u, w) needs u in row w (rows ascending: a binary search).  *bad is set on
+// the first violation.
+__global__ void check_symmetric_kernel(const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
+                                       const int32_t *__restrict__ rowid, int64_t nnz, int *bad) {
+    GRID_STRIDE(j, nnz) {
+        const int u = rowid[j], w = col[j];
+        int lo = rp[w], hi = rp[w + 1];
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (col[mid] < u) lo = mid + 1;
+            else hi = mid;
+        }
+        if (u == w || lo == rp[w + 1] || col[lo] != u) *bad = 1;
+    }
+}
+
 // rowid[j] = u for j in row u (one warp per row)
 __global__ void rowid_kernel(const int32_t *rp, int64_t n_rows, int32_t *rowid) {
     const int lane = threadIdx.x & 31;
@@ -254,6 +271,45 @@ __global__ void __launch_bounds__(kOT) orient_tile_write_kernel(const int32_t *_
 }
 
 // ---- halo ----------------------------------------------------------------------
+// Halo sets of all parts (k <= 32) in one pass: mask[v] gets bit q for every
+// neighbour of v in part q, so v is in part p's halo when bit p is set and
+// part[v] != p (the undirected CSR is symmetric: v has a neighbour in p iff
+// some vertex of p has v as a neighbour).  One atomicOr per row run of a
+// thread's 16 entries.
+__global__ void __launch_bounds__(kOT) halo_mask_kernel(const int32_t *__restrict__ rowid,
+                                                         const int32_t *__restrict__ col,
+                                                         const int32_t *__restrict__ part, int64_t nnz,
+                                                         unsigned *__restrict__ mask) {
+    int u[kOI], w[kOI];
+    const int64_t j0 = (int64_t)blockIdx.x * kOTile + (int64_t)threadIdx.x * kOI;
+    if (j0 >= nnz) return;
+    load16(rowid, col, j0, nnz, u, w);
+    int cur = u[0];
+    unsigned m = 0;
+#pragma unroll
+    for (int i = 0; i < kOI; ++i) {
+        if (j0 + i >= nnz) break;
+        if (u[i] != cur) {
+            if (m) atomicOr(mask + cur, m);
+            cur = u[i];
+            m = 0;
+        }
+        const unsigned q = (unsigned)__ldg(part + w[i]);
+        if (q < 32u) m |= 1u << q;
+    }
+    if (m) atomicOr(mask + cur, m);
+}
+
+__global__ void part_halo_flags_kernel(const int32_t *part, const unsigned *mask, int64_t n, int p, uint8_t *inP,
+                                       uint8_t *inH) {
+    GRID_STRIDE(v, n) {
+        const bool in = part[v] == p;
+        inP[v] = (uint8_t)in;
+        inH[v] = (uint8_t)(!in && ((mask[v] >> p) & 1u));
+    }
+}
+
+// More than 32 parts: part p's flags, and its halo by one pass over the entries.
 __global__ void part_flags_kernel(const int32_t *part, int64_t n, int p, uint8_t *inP) {
     GRID_STRIDE(v, n) inP[v] = (uint8_t)(part[v] == p);
 }
@@ -266,9 +322,38 @@ __global__ void halo_flags_kernel(const int32_t *rowid, const int32_t *col, int6
     }
 }
 
+// ld[v] = (local id or -1, degree): the tile passes gather both with one load.
 __global__ void local_ids_kernel(const uint8_t *inP, const uint8_t *inH, const int32_t *lidP, const int32_t *lidH,
-                                 int64_t n, int t_ver, int32_t *lid) {
-    GRID_STRIDE(v, n) lid[v] = inP[v] ? lidP[v] : (inH[v] ? t_ver + lidH[v] : -1);
+                                 const int32_t *deg, int64_t n, int t_ver, int2 *ld) {
+    GRID_STRIDE(v, n) ld[v] = make_int2(inP[v] ? lidP[v] : (inH[v] ? t_ver + lidH[v] : -1), deg[v]);
+}
+
+// Exclusive scan of one 64-bit value per thread over a 256-thread block.
+__device__ __forceinline__ unsigned long long block_scan_256_u64(unsigned long long v, unsigned long long *total) {
+    __shared__ unsigned long long wsum[kOT / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long t = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += t;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long w = lane < kOT / 32 ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < kOT / 32; o <<= 1) {
+            const unsigned long long t = __shfl_up_sync(kFull, w, o);
+            if (lane >= o) w += t;
+        }
+        if (lane < kOT / 32) wsum[lane] = w;
+    }
+    __syncthreads();
+    const unsigned long long excl = x - v + (warp ? wsum[warp - 1] : 0);
+    *total = wsum[kOT / 32 - 1];
+    __syncthreads();
+    return excl;
 }
 
 // Local edges over the orientation's 4096-entry tiles.  Entry j (row s, id d)
@@ -279,51 +364,57 @@ __global__ void local_ids_kernel(const uint8_t *inP, const uint8_t *inH, const i
 // row is its rank among the row's entries of its class (plus the row's P count
 // for an H entry).  Ranks come from the tiles' P and H counts, scanned, and one
 // block scan per tile, as in the orientation; no per-entry flag or position
-// array is written.
+// array is written.  A third class, R, counts the halo in-degrees without
+// atomics: entry j of a halo row s is an R entry when d has a local id and
+// d -> s is the oriented direction, so s's in-degree is its row's R count.
 //
-// Pass 1 stores the 32 class bits of each thread's 16 entries (P in the low
-// half, H in the high half), the tile's P and H counts (tile_cnt[t] and
-// tile_cnt[tiles + t]) and every row's P and H ranks within the tile of its
-// start (packed 16 + 16 bits: a tile holds 4096 entries), and counts each halo
-// vertex's in-degree (its H entries) for the prune.
+// Pass 1 stores the P and H bits of each thread's 16 entries (P in the low
+// half, H in the high half), the tile's P, H and R counts (tile_cnt[c * tiles +
+// t]) and every row's P, H and R ranks within the tile of its start (16 bits
+// each, packed: a tile holds 4096 entries).
+constexpr int kRankBits = 16;
+constexpr unsigned long long kRankMask = (1ull << kRankBits) - 1ull;
+
 __global__ void __launch_bounds__(kOT) halo_tile_count_kernel(const int32_t *__restrict__ rowid,
                                                                const int32_t *__restrict__ col,
-                                                               const int32_t *__restrict__ deg,
-                                                               const int32_t *__restrict__ lid, int64_t nnz, int64_t V,
+                                                               const int2 *__restrict__ ld, int64_t nnz, int64_t V,
                                                                int64_t tiles, int t_ver, int tie,
                                                                uint32_t *__restrict__ bits,
                                                                int32_t *__restrict__ tile_cnt,
-                                                               uint32_t *__restrict__ row_rank,
-                                                               int32_t *__restrict__ indeg) {
+                                                               unsigned long long *__restrict__ row_rank) {
     int u[kOI], w[kOI];
     const int64_t j0 = (int64_t)blockIdx.x * kOTile + (int64_t)threadIdx.x * kOI;
     load16(rowid, col, j0, nnz, u, w);
-    unsigned pb = 0, hb = 0;
-    int cs = -1, cls = -1, cdeg = 0;  // the current row: id, local id, degree
+    unsigned pb = 0, hb = 0, rb = 0;
+    int cs = -1;
+    int2 cx = make_int2(-1, 0);  // the current row: local id, degree
 #pragma unroll
     for (int i = 0; i < kOI; ++i) {
         if (j0 + i >= nnz) break;
         if (u[i] != cs) {
             cs = u[i];
-            cls = __ldg(lid + cs);
-            cdeg = __ldg(deg + cs);
+            cx = __ldg(ld + cs);
         }
-        if (cls < 0) continue;
-        const int ld = __ldg(lid + w[i]);
-        if (ld < 0 || !keep_edge(cdeg, __ldg(deg + w[i]), cs, w[i], tie)) continue;
-        if (ld < t_ver) {
-            pb |= 1u << i;
-        } else {
-            hb |= 1u << i;
-            atomicAdd(indeg + ld, 1);
+        if (cx.x < 0) continue;
+        const int2 wx = __ldg(ld + w[i]);
+        if (wx.x < 0) continue;
+        if (keep_edge(cx.y, wx.y, cs, w[i], tie)) {
+            if (wx.x < t_ver) pb |= 1u << i;
+            else hb |= 1u << i;
+        } else if (cx.x >= t_ver) {
+            rb |= 1u << i;
         }
     }
     bits[(int64_t)blockIdx.x * kOT + threadIdx.x] = pb | (hb << 16);
-    int total = 0;
-    const int excl = block_scan_256((int)(__popc(pb) | (__popc(hb) << 16)), &total);
+    auto pack = [](unsigned a, unsigned b, unsigned c) {
+        return (unsigned long long)a | ((unsigned long long)b << kRankBits) | ((unsigned long long)c << (2 * kRankBits));
+    };
+    unsigned long long total = 0;
+    const unsigned long long excl = block_scan_256_u64(pack(__popc(pb), __popc(hb), __popc(rb)), &total);
     if (threadIdx.x == 0) {
-        tile_cnt[blockIdx.x] = total & 0xffff;
-        tile_cnt[tiles + blockIdx.x] = total >> 16;
+        tile_cnt[blockIdx.x] = (int)(total & kRankMask);
+        tile_cnt[tiles + blockIdx.x] = (int)((total >> kRankBits) & kRankMask);
+        tile_cnt[2 * tiles + blockIdx.x] = (int)(total >> (2 * kRankBits));
     }
     if (j0 >= nnz) return;
     int prev = j0 == 0 ? -1 : __ldg(rowid + j0 - 1);
@@ -332,42 +423,44 @@ __global__ void __launch_bounds__(kOT) halo_tile_count_kernel(const int32_t *__r
         if (j0 + i >= nnz) break;
         if (u[i] == prev) continue;
         const unsigned below = (1u << i) - 1u;
-        const uint32_t rk = (uint32_t)excl + (__popc(pb & below) | (__popc(hb & below) << 16));
+        const unsigned long long rk = excl + pack(__popc(pb & below), __popc(hb & below), __popc(rb & below));
         for (int r = prev + 1; r <= u[i]; ++r) row_rank[r] = rk;  // rows that start at this entry
         prev = u[i];
     }
     if (j0 + kOI >= nnz) {  // the last entry's thread: the rows after it (and row V) start at the end
-        const uint32_t rk = (uint32_t)excl + (__popc(pb) | (__popc(hb) << 16));
+        const unsigned long long rk = excl + pack(__popc(pb), __popc(hb), __popc(rb));
         for (int64_t r = (int64_t)prev + 1; r <= V; ++r) row_rank[r] = rk;
     }
 }
 
-// Global P and H ranks of entry index a, whose row-start rank (within the tile
-// of a; the last tile for a = nnz) is rk.  off[] is the exclusive scan of the
-// 2 * tiles tile counts.
-__device__ __forceinline__ void halo_rank(int a, uint32_t rk, const int32_t *off, int64_t tiles, int &pr, int &hr) {
+// Global rank of class c (0 = P, 1 = H, 2 = R) at entry index a, whose row-start
+// rank (within the tile of a; the last tile for a = nnz) is rk.  off[] is the
+// exclusive scan of the 3 * tiles tile counts.
+__device__ __forceinline__ int halo_rank(int a, unsigned long long rk, const int32_t *off, int64_t tiles, int c) {
     const int64_t t = min((int64_t)(a / kOTile), tiles - 1);
-    pr = off[t] + (int)(rk & 0xffffu);
-    hr = off[tiles + t] - off[tiles] + (int)(rk >> 16);
+    return off[c * tiles + t] - off[c * tiles] + (int)((rk >> (c * kRankBits)) & kRankMask);
 }
 
 // Per vertex of the part's combined set: its P and H entry counts (from the
-// ranks at its row's start and at the next row's start) -> cnt[local id], and
-// the bases that turn an entry's global rank into its local-row offset.
-__global__ void halo_rows_kernel(const int32_t *__restrict__ rp, const int32_t *__restrict__ lid,
-                                 const uint32_t *__restrict__ row_rank, const int32_t *__restrict__ off, int64_t V,
-                                 int64_t tiles, int32_t *__restrict__ cnt, int32_t *__restrict__ base_p,
-                                 int32_t *__restrict__ base_h) {
+// ranks at its row's start and at the next row's start) -> cnt[local id], the
+// bases that turn an entry's global rank into its local-row offset, and the
+// in-degree of a halo vertex (its row's R count; 0 for a part vertex).
+__global__ void halo_rows_kernel(const int32_t *__restrict__ rp, const int2 *__restrict__ ld,
+                                 const unsigned long long *__restrict__ row_rank, const int32_t *__restrict__ off,
+                                 int64_t V, int64_t tiles, int t_ver, int32_t *__restrict__ cnt,
+                                 int32_t *__restrict__ base_p, int32_t *__restrict__ base_h,
+                                 int32_t *__restrict__ indeg) {
     GRID_STRIDE(v, V) {
-        const int l = lid[v];
+        const int l = ld[v].x;
         if (l < 0) continue;
-        int pa, ha, pb, hb;
-        halo_rank(rp[v], row_rank[v], off, tiles, pa, ha);
-        halo_rank(rp[v + 1], row_rank[v + 1], off, tiles, pb, hb);
-        const int np = pb - pa;
-        cnt[l] = np + (hb - ha);
+        const int a = rp[v], b = rp[v + 1];
+        const unsigned long long ra = row_rank[v], rb = row_rank[v + 1];
+        const int pa = halo_rank(a, ra, off, tiles, 0), np = halo_rank(b, rb, off, tiles, 0) - pa;
+        const int ha = halo_rank(a, ra, off, tiles, 1), nh = halo_rank(b, rb, off, tiles, 1) - ha;
+        cnt[l] = np + nh;
         base_p[v] = pa;       // P entry of rank x: local offset x - pa
         base_h[v] = ha - np;  // H entry of rank x: local offset np + (x - ha)
+        indeg[l] = l >= t_ver ? halo_rank(b, rb, off, tiles, 2) - halo_rank(a, ra, off, tiles, 2) : 0;
     }
 }
 
@@ -376,7 +469,7 @@ __global__ void halo_rows_kernel(const int32_t *__restrict__ rp, const int32_t *
 // of the target, lrow = the local row, for the prune's compaction).
 __global__ void __launch_bounds__(kOT) halo_tile_write_kernel(const int32_t *__restrict__ rowid,
                                                                const int32_t *__restrict__ col,
-                                                               const int32_t *__restrict__ lid,
+                                                               const int2 *__restrict__ ld,
                                                                const uint32_t *__restrict__ bits, int64_t nnz,
                                                                int64_t tiles, const int32_t *__restrict__ off,
                                                                const int32_t *__restrict__ lrp,
@@ -400,13 +493,13 @@ __global__ void __launch_bounds__(kOT) halo_tile_write_kernel(const int32_t *__r
         if (!(b & (bit | (bit << 16)))) continue;
         if (u[i] != cs) {
             cs = u[i];
-            ls = __ldg(lid + cs);
+            ls = __ldg(ld + cs).x;
             const int lr = __ldg(lrp + ls);
             offp = lr - __ldg(base_p + cs);
             offh = lr - __ldg(base_h + cs);
         }
         const int o = (pb & bit) ? offp + pr++ : offh + hr++;
-        lcol[o] = __ldg(lid + w[i]);
+        lcol[o] = __ldg(ld + w[i]).x;
         lrow[o] = ls;
     }
 }
@@ -636,6 +729,12 @@ int tc_ugraph_upload_i64(tc_ctx *ctx, const int64_t *row_ptr, const int64_t *col
         rowid_kernel<<<grid(n_rows * 32, ctx), 256, 0, s>>>(rp.p, n_rows, rowid.p);
         TC_CUDA(cudaGetLastError());
     }
+    if (nnz) {  // the halo extraction reads each edge from either end
+        check_symmetric_kernel<<<grid(nnz, ctx), 256, 0, s>>>(rp.p, cl.p, rowid.p, nnz, bad.p);
+        TC_CUDA(cudaGetLastError());
+        TC_TRY(d2h_scalar(&hbad, bad.p, s));
+        if (hbad) return set_error(TC_E_INVALID, "undirected CSR has a self-loop or an edge missing from one of its rows");
+    }
     TC_CUDA(cudaStreamSynchronize(s));
     return finish_ugraph(ctx, rp.release(), cl.release(), dg.release(), rowid.release(), n_rows, nnz, out);
 }
@@ -736,8 +835,10 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
     for (int64_t v = 0; v < V; ++v)
         if (part[v] < 0) return set_error(TC_E_RANGE, "part[%lld] = %d is negative", (long long)v, part[v]);
     const int64_t tiles = (nnz + kOTile - 1) / kOTile;
-    DBuf<int32_t> dpart, lidP, lidH, lid, cnt, lrp, tile_cnt, tile_off, base_p, base_h;
-    DBuf<uint32_t> bits, row_rank;
+    DBuf<int32_t> dpart, lidP, lidH, cnt, lrp, tile_cnt, tile_off, base_p, base_h;
+    DBuf<int2> ld;
+    DBuf<uint32_t> bits, mask;
+    DBuf<unsigned long long> row_rank;
     DBuf<uint8_t> inP, inH;
     TC_TRY(dpart.alloc((size_t)std::max<int64_t>(V, 1), s));
     if (V) TC_CUDA(cudaMemcpyAsync(dpart.p, part, sizeof(int32_t) * (size_t)V, cudaMemcpyHostToDevice, s));
@@ -745,21 +846,32 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
     TC_TRY(inH.alloc((size_t)V, s));
     TC_TRY(lidP.alloc((size_t)V + 1, s));
     TC_TRY(lidH.alloc((size_t)V + 1, s));
-    TC_TRY(lid.alloc((size_t)std::max<int64_t>(V, 1), s));
+    TC_TRY(ld.alloc((size_t)std::max<int64_t>(V, 1), s));
     TC_TRY(cnt.alloc((size_t)V + 1, s));
     TC_TRY(lrp.alloc((size_t)V + 1, s));
     TC_TRY(base_p.alloc((size_t)std::max<int64_t>(V, 1), s));
     TC_TRY(base_h.alloc((size_t)std::max<int64_t>(V, 1), s));
     TC_TRY(row_rank.alloc((size_t)V + 1, s));
     TC_TRY(bits.alloc((size_t)std::max<int64_t>(tiles, 1) * kOT, s));
-    TC_TRY(tile_cnt.alloc((size_t)std::max<int64_t>(2 * tiles, 1), s));
-    TC_TRY(tile_off.alloc((size_t)2 * tiles + 1, s));
+    TC_TRY(tile_cnt.alloc((size_t)std::max<int64_t>(3 * tiles, 1), s));
+    TC_TRY(tile_off.alloc((size_t)3 * tiles + 1, s));
     const int gV = grid(V, ctx), gE = grid(nnz, ctx);
+    const bool masks = k <= 32;  // every part's halo from one pass
+    if (masks) {
+        TC_TRY(mask.alloc((size_t)std::max<int64_t>(V, 1), s));
+        TC_CUDA(cudaMemsetAsync(mask.p, 0, sizeof(uint32_t) * (size_t)std::max<int64_t>(V, 1), s));
+        if (tiles) halo_mask_kernel<<<(unsigned)tiles, kOT, 0, s>>>(ug->rowid, ug->col, dpart.p, nnz, mask.p);
+        TC_CUDA(cudaGetLastError());
+    }
     // one part; any failure returns its status (the caller frees all parts)
     auto one_part = [&](int p) -> int {
-        if (V) part_flags_kernel<<<gV, 256, 0, s>>>(dpart.p, V, p, inP.p);
-        TC_CUDA(cudaMemsetAsync(inH.p, 0, (size_t)V, s));
-        if (nnz) halo_flags_kernel<<<gE, 256, 0, s>>>(ug->rowid, ug->col, nnz, dpart.p, p, inH.p);
+        if (masks) {
+            if (V) part_halo_flags_kernel<<<gV, 256, 0, s>>>(dpart.p, mask.p, V, p, inP.p, inH.p);
+        } else {
+            if (V) part_flags_kernel<<<gV, 256, 0, s>>>(dpart.p, V, p, inP.p);
+            TC_CUDA(cudaMemsetAsync(inH.p, 0, (size_t)V, s));
+            if (nnz) halo_flags_kernel<<<gE, 256, 0, s>>>(ug->rowid, ug->col, nnz, dpart.p, p, inH.p);
+        }
         TC_CUDA(cudaGetLastError());
         TC_TRY(scan_flags_u8(inP.p, lidP.p, V, s));
         TC_TRY(scan_flags_u8(inH.p, lidH.p, V, s));
@@ -768,22 +880,21 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
         TC_CUDA(cudaMemcpyAsync(&n_halo, lidH.p + V, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         TC_CUDA(cudaStreamSynchronize(s));
         const int64_t n_comb = (int64_t)t_ver + n_halo;
-        if (V) local_ids_kernel<<<gV, 256, 0, s>>>(inP.p, inH.p, lidP.p, lidH.p, V, t_ver, lid.p);
+        if (V) local_ids_kernel<<<gV, 256, 0, s>>>(inP.p, inH.p, lidP.p, lidH.p, ug->deg, V, t_ver, ld.p);
         DBuf<int32_t> indeg;
         TC_TRY(indeg.alloc((size_t)std::max<int64_t>(n_comb, 1), s));
-        TC_CUDA(cudaMemsetAsync(indeg.p, 0, sizeof(int32_t) * (size_t)std::max<int64_t>(n_comb, 1), s));
         if (tiles) {
-            halo_tile_count_kernel<<<(unsigned)tiles, kOT, 0, s>>>(ug->rowid, ug->col, ug->deg, lid.p, nnz, V, tiles,
-                                                                    t_ver, tie, bits.p, tile_cnt.p, row_rank.p,
-                                                                    indeg.p);
+            halo_tile_count_kernel<<<(unsigned)tiles, kOT, 0, s>>>(ug->rowid, ug->col, ld.p, nnz, V, tiles, t_ver, tie,
+                                                                    bits.p, tile_cnt.p, row_rank.p);
             TC_CUDA(cudaGetLastError());
-            TC_TRY(scan_exclusive_i32(tile_cnt.p, tile_off.p, 2 * tiles, s));
+            TC_TRY(scan_exclusive_i32(tile_cnt.p, tile_off.p, 3 * tiles, s));
             if (V)
-                halo_rows_kernel<<<gV, 256, 0, s>>>(ug->rp, lid.p, row_rank.p, tile_off.p, V, tiles, cnt.p, base_p.p,
-                                                    base_h.p);
+                halo_rows_kernel<<<gV, 256, 0, s>>>(ug->rp, ld.p, row_rank.p, tile_off.p, V, tiles, t_ver, cnt.p,
+                                                    base_p.p, base_h.p, indeg.p);
             TC_CUDA(cudaGetLastError());
         } else {
             TC_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * ((size_t)n_comb + 1), s));
+            TC_CUDA(cudaMemsetAsync(indeg.p, 0, sizeof(int32_t) * (size_t)std::max<int64_t>(n_comb, 1), s));
         }
         TC_TRY(scan_exclusive_i32(cnt.p, lrp.p, n_comb, s));
         int32_t lnnz = 0;
@@ -793,7 +904,7 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
         TC_TRY(lcol.alloc((size_t)lnnz, s));
         TC_TRY(lrow.alloc((size_t)lnnz, s));
         if (tiles && lnnz)
-            halo_tile_write_kernel<<<(unsigned)tiles, kOT, 0, s>>>(ug->rowid, ug->col, lid.p, bits.p, nnz, tiles,
+            halo_tile_write_kernel<<<(unsigned)tiles, kOT, 0, s>>>(ug->rowid, ug->col, ld.p, bits.p, nnz, tiles,
                                                                     tile_off.p, lrp.p, base_p.p, base_h.p, lcol.p,
                                                                     lrow.p);
         TC_CUDA(cudaGetLastError());
