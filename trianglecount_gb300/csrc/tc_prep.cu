@@ -11,11 +11,12 @@
 //   kept entries and the new row starts, so rows stay ascending.
 // Halo extraction restates create_subgraph_with_halo
 // (preprocess_GPU/Halo_cleanned_preprocess/round_clean_subgraph.cu:357-902) with the
-// intended prune loop of Halo_creation_preprocess.py:566-589: per part, local
-// ids (part vertices, then halo, each ascending) -> P/H class bits, tile counts,
-// row-start ranks and halo in-degrees over the orientation's tiles -> scan ->
-// local row lengths -> scan -> ordered write of every local edge; then halo
-// vertices with zero in-degree are peeled until none is left.
+// intended prune loop of Halo_creation_preprocess.py:566-589: the halo sets of
+// all parts from one pass (k <= 32); per part, local ids (part vertices, then
+// halo, each ascending) -> P/H/R class bits, tile counts and row-start ranks
+// over the orientation's tiles -> scan -> local row lengths and halo in-degrees
+// -> scan -> ordered write of every local edge; then halo vertices with zero
+// in-degree are peeled until none is left.
 #include <algorithm>
 #include <vector>
 
