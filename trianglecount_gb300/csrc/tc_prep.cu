@@ -563,10 +563,24 @@ __global__ void frontier_init_kernel(const int32_t *indeg, int64_t n, int t_ver,
     }
 }
 
-// one warp per frontier vertex: drop its out-edges; halo targets reaching
-// in-degree 0 join the next frontier (exactly once: the 1 -> 0 transition).
-__global__ void peel_kernel(const int32_t *front, int n_front, const int32_t *lrp, const int32_t *lcol, int t_ver,
-                            int32_t *indeg, uint8_t *removed, int32_t *next, int32_t *next_n) {
+// Peel round r, one warp per frontier vertex: drop its out-edges; halo targets
+// reaching in-degree 0 join the next frontier (exactly once: the 1 -> 0
+// transition).  Frontier sizes stay on the device so that several rounds go
+// out per host check: fn[r % 3] is round r's frontier size (front_a for even r,
+// front_b for odd r), fn[(r + 1) % 3] (zeroed by round r - 1, or before round 0)
+// counts the next frontier, and fn[(r + 2) % 3], which no block of round r
+// reads, is zeroed for round r + 1.  fn[3] totals the frontier sizes.  A round
+// whose frontier is empty does nothing.
+__global__ void peel_round_kernel(int32_t *front_a, int32_t *front_b, int32_t *fn, int r, const int32_t *lrp,
+                                  const int32_t *lcol, int t_ver, int32_t *indeg, uint8_t *removed) {
+    const int32_t *front = (r & 1) ? front_b : front_a;
+    int32_t *next = (r & 1) ? front_a : front_b;
+    const int n_front = fn[r % 3];
+    int32_t *next_n = fn + (r + 1) % 3;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        fn[(r + 2) % 3] = 0;
+        fn[3] += n_front;
+    }
     const int lane = threadIdx.x & 31;
     const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -961,23 +975,27 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
         TC_TRY(removed.alloc((size_t)std::max<int64_t>(n_comb, 1), s));
         TC_TRY(front.alloc((size_t)std::max<int32_t>(n_halo, 1), s));
         TC_TRY(next.alloc((size_t)std::max<int32_t>(n_halo, 1), s));
-        TC_TRY(fn.alloc(2, s));
+        TC_TRY(fn.alloc(4, s));
         TC_CUDA(cudaMemsetAsync(removed.p, 0, (size_t)std::max<int64_t>(n_comb, 1), s));
-        TC_CUDA(cudaMemsetAsync(fn.p, 0, 2 * sizeof(int32_t), s));
+        TC_CUDA(cudaMemsetAsync(fn.p, 0, 4 * sizeof(int32_t), s));
         if (n_comb) frontier_init_kernel<<<grid(n_comb, ctx), 256, 0, s>>>(indeg.p, n_comb, t_ver, removed.p, front.p, fn.p);
         TC_CUDA(cudaGetLastError());
-        int32_t n_front = 0, n_removed = 0;
-        TC_TRY(d2h_scalar(&n_front, fn.p, s));
-        // each round removes at least one halo vertex, so at most n_halo rounds
-        for (int round = 0; n_front > 0 && round <= n_halo; ++round) {
-            n_removed += n_front;
-            TC_CUDA(cudaMemsetAsync(fn.p + 1, 0, sizeof(int32_t), s));
-            peel_kernel<<<grid((int64_t)n_front * 32, ctx), 256, 0, s>>>(front.p, n_front, lrp.p, lcol.p, t_ver, indeg.p,
-                                                                         removed.p, next.p, fn.p + 1);
+        // kPeelBatch rounds per host check; each non-empty round removes at
+        // least one halo vertex, so at most n_halo of them are non-empty
+        constexpr int kPeelBatch = 4;
+        const int peel_grid = std::min(grid((int64_t)std::max<int32_t>(n_halo, 1) * 32, ctx), ctx->sm_count * 4);
+        int32_t hfn[4] = {0, 0, 0, 0};
+        int round = 0;
+        while (round <= n_halo) {
+            for (int q = 0; q < kPeelBatch; ++q, ++round)
+                peel_round_kernel<<<peel_grid, 256, 0, s>>>(front.p, next.p, fn.p, round, lrp.p, lcol.p, t_ver, indeg.p,
+                                                            removed.p);
             TC_CUDA(cudaGetLastError());
-            TC_TRY(d2h_scalar(&n_front, fn.p + 1, s));
-            std::swap(front.p, next.p);
+            TC_CUDA(cudaMemcpyAsync(hfn, fn.p, sizeof(hfn), cudaMemcpyDeviceToHost, s));
+            TC_CUDA(cudaStreamSynchronize(s));
+            if (hfn[round % 3] == 0) break;  // the next round's frontier is empty
         }
+        const int64_t n_removed = (int64_t)hfn[3] + hfn[round % 3];
         int32_t *out_rp = nullptr, *out_col = nullptr;
         int64_t n_local = n_comb, out_nnz = lnnz;
         if (n_removed == 0) {
