@@ -356,7 +356,8 @@ def run_ours(args, world, rank, local, pg):
                     "gpu_launches": (launches_per_count + 2) * args.steps},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": f"{peak_src} hbm_gbs (copy, burst)",
-                         "kernel": "flat_kernel" if flat else "count_kernel", "kernel_ms": kernel_avg_ms,
+                         "kernel": (("flat4_kernel" if int(dplus.max(initial=0)) <= 4 else "flat_kernel") if flat
+                                    else "count_kernel"), "kernel_ms": kernel_avg_ms,
                          "algorithmic_bytes_per_launch": B_alg,
                          "algorithmic_bytes_definition": "4(V+1) + 12|E+| + 4 W+ + 8, W+ = sum over oriented "
                                                          "edges of d+(v): each root's row_ptr and list once, "
