@@ -143,7 +143,7 @@ int ensure_count_scratch(tc_graph *g) {
     }
     if (!g->d_desc) {  // the flat count needs only the work words
         TC_TRY(dalloc((void **)&g->d_desc, sizeof(GraphDesc), ctx->stream));
-        TC_TRY(scratch_alloc(&g->sc, g->n_rows + 1, (g->n_rows + 31) / 32, g->nnz,
+        TC_TRY(scratch_alloc(&g->sc, g->n_rows + 1, g->nnz,
                              std::min(g->n_rows, g->nnz) + 1, ctx->stream));
     }
     return TC_OK;
@@ -256,11 +256,10 @@ void ctx_release(tc_ctx *c) {
     delete c;
 }
 
-int scratch_alloc(CountScratch *sc, int64_t V, int64_t C, int64_t E, int64_t heavy_cap, cudaStream_t s) {
+int scratch_alloc(CountScratch *sc, int64_t V, int64_t E, int64_t heavy_cap, cudaStream_t s) {
     sc->heavy_cap = heavy_cap;
     TC_TRY(dalloc((void **)&sc->heavy, sizeof(HeavyEntry) * (size_t)std::max<int64_t>(heavy_cap, 1), s));
     TC_TRY(dalloc((void **)&sc->light_list, sizeof(uint32_t) * (size_t)std::max<int64_t>(V, 1), s));
-    TC_TRY(dalloc((void **)&sc->micro_mask, sizeof(uint32_t) * (size_t)std::max<int64_t>(C, 1), s));
     TC_TRY(dalloc((void **)&sc->in_cnt, sizeof(int32_t) * (size_t)std::max<int64_t>(V, 1), s));
     TC_TRY(dalloc((void **)&sc->in_off, sizeof(int32_t) * (size_t)(V + 1), s));
     TC_TRY(dalloc((void **)&sc->in_work, sizeof(unsigned long long) * (size_t)std::max<int64_t>(V, 1), s));
@@ -273,7 +272,6 @@ int scratch_alloc(CountScratch *sc, int64_t V, int64_t C, int64_t E, int64_t hea
 void scratch_free(CountScratch *sc, cudaStream_t s) {
     dfree(sc->heavy, s);
     dfree(sc->light_list, s);
-    dfree(sc->micro_mask, s);
     dfree(sc->in_cnt, s);
     dfree(sc->in_off, s);
     dfree(sc->in_work, s);
@@ -298,7 +296,7 @@ int graph_rebind(tc_graph *g, tc_ctx *ctx) {
 
 size_t graph_device_bytes(const tc_graph *g) {
     const size_t csr = sizeof(int32_t) * (size_t)(g->n_rows + 1 + g->nnz);
-    const size_t scratch = (size_t)(g->n_rows + 1) * (4 + 4 + 8 + 8 + 4 + 16 + 1) + (size_t)g->nnz * 5 + 1024;
+    const size_t scratch = (size_t)(g->n_rows + 1) * (4 + 4 + 8 + 8 + 4 + 16) + (size_t)g->nnz * 5 + 1024;
     return csr + scratch;
 }
 
@@ -339,7 +337,7 @@ int count_graphs_direct(tc_ctx *ctx, tc_graph *const *graphs, int n, uint64_t *o
     }
     int st = d_desc.alloc((size_t)n, s);
     if (st == TC_OK) st = d_work.alloc(out_bytes, s);
-    if (st == TC_OK) st = scratch_alloc(&sc, vtot, chunks, etot, cap, s);
+    if (st == TC_OK) st = scratch_alloc(&sc, vtot, etot, cap, s);
     if (st == TC_OK && cudaMemcpyAsync(d_desc.p, desc.data(), sizeof(GraphDesc) * (size_t)n, cudaMemcpyHostToDevice,
                                        s) != cudaSuccess)
         st = set_error(TC_E_CUDA, "descriptor upload failed");
@@ -830,7 +828,7 @@ int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out)
     b->total_chunks = chunks;
     b->total_vertices = vtot;
     int st = dalloc((void **)&b->d_desc, sizeof(GraphDesc) * (size_t)n, s);
-    if (st == TC_OK) st = scratch_alloc(&b->sc, vtot, chunks, etot, cap, s);
+    if (st == TC_OK) st = scratch_alloc(&b->sc, vtot, etot, cap, s);
     if (st == TC_OK) st = dalloc((void **)&b->d_work, sizeof(CountWork) + sizeof(unsigned long long) * (size_t)n, s);
     if (st == TC_OK && cudaMallocHost(&b->h_out, sizeof(CountWork) + sizeof(unsigned long long) * (size_t)n) != cudaSuccess)
         st = set_error(TC_E_NOMEM, "pinned result buffer");

@@ -36,12 +36,13 @@
 //   scan       in-edge offsets
 //   transpose  per root u, scatter the middle-centric edges into the in-lists;
 //              classify each vertex x by d+(x) and its work w(x): micro tasks
-//              (d+(x) <= 8, w(x) <= 128) are marked in a 32-bit mask per
-//              chunk, light tasks (d+(x) <= warp_max, w(x) <= the light bound)
-//              are appended to a list, heavy ones become (#tiles x #slices)
+//              (d+(x) <= 8, w(x) <= 128) are listed from the top of the task
+//              list, light tasks (d+(x) <= warp_max, w(x) <= the light bound)
+//              from its bottom, heavy ones become (#tiles x #slices)
 //              block units, appended with one packed 64-bit atomic so entries
 //              stay sorted by unit
-//   micro      one lane per micro task, N+(x) in registers
+//   micro      one lane per listed micro task (a warp takes 32), N+(x) in
+//              registers
 //   count      persistent grid (SMs x occupancy blocks):
 //                phase A -- blocks pull heavy units from a global cursor; a
 //                  unit hashes one tile of N+(x) (load factor <= 1/4) in shared
@@ -262,8 +263,9 @@ struct KParams {
     int64_t heavy_cap;
     CountWork *work;
     unsigned long long *results;
-    uint32_t *light_list;  // light tasks (chunk * 32 + lane), work->n_light of them
-    uint32_t *micro_mask;  // one word per 32-row chunk
+    uint32_t *light_list;  // tasks as global rows chunk * 32 + lane: work->n_light light tasks from
+                           // entry 0 up, work->n_micro micro tasks from entry list_cap - 1 down
+    int64_t list_cap;      // entries of light_list (the launch's rows: a row is at most one task)
     int32_t *in_cnt;       // per vertex (pooled): d+ during in_count, then middle-centric in-edges (split from in_work)
     int32_t *in_off;       // per vertex (pooled) + 1: exclusive scan of in_cnt
     unsigned long long *in_work;   // per vertex: (in-edges << 32) | sum of d+(u) over its in-partners u;
@@ -521,8 +523,9 @@ __global__ void __launch_bounds__(kThreads) split_in_count_kernel(const unsigned
 }
 
 // transpose + classify: scatter the chunk's middle-centric edges into the
-// in-lists, then classify each row of the chunk as a micro task (mask), a
-// light task (list), a heavy task (block units) or no work.
+// in-lists, then classify each row of the chunk as a micro task (task list,
+// from the top), a light task (task list, from the bottom), a heavy task
+// (block units) or no work.
 __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P, HeavyEntry *heavy) {
     const int lane = threadIdx.x & (kWarp - 1);
     // Block-unit size: unit_work, or less on a small job so that every count
@@ -585,7 +588,14 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
             const bool hv = has && !micro && !light;
             const uint32_t mm = __ballot_sync(kFull, micro);
             const uint32_t lm = __ballot_sync(kFull, light);
-            if (lane == 0) P.micro_mask[c] = mm;
+            if (mm) {  // list the chunk's micro tasks from the top (one atomic per chunk)
+                unsigned base = 0;
+                if (lane == 0) base = atomicAdd(&P.work->n_micro, (unsigned)__popc(mm));
+                base = __shfl_sync(kFull, base, 0);
+                if (micro)
+                    P.light_list[P.list_cap - 1 - (int64_t)(base + __popc(mm & ((1u << lane) - 1u)))] =
+                        (uint32_t)(c * kWarp + lane);
+            }
             if (lm) {  // list the chunk's light tasks (one atomic per chunk)
                 unsigned base = 0;
                 if (lane == 0) base = atomicAdd(&P.work->n_light, (unsigned)__popc(lm));
@@ -701,34 +711,40 @@ __device__ __forceinline__ uint32_t micro_task(const KParams &P, const GraphDesc
 template <bool kPerRoot>
 __global__ void __launch_bounds__(kThreads) micro_kernel(KParams P) {
     const int lane = threadIdx.x & (kWarp - 1);
-    unsigned long long acc = 0;
+    const int64_t n = P.work->n_micro;
+    const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / kWarp;
+    unsigned long long acc = 0;  // this lane's hits for graph cur_g
     int cur_g = -1;
-    int64_t c, c_end;
-    aux_next(P, 2, lane, true, c, c_end);
-    for (; c < c_end; aux_next(P, 2, lane, false, c, c_end)) {
-        for (; c < c_end; ++c) {
-            const uint32_t mm = P.micro_mask[c];
-            if (!mm) continue;
-            const int g = find_graph(P.gd, P.n_graphs, c);
-            const GraphDesc &G = P.gd[g];
-            if (!kPerRoot && g != cur_g) {
-                const unsigned long long s = warp_sum_u64(acc);
-                if (lane == 0 && cur_g >= 0 && s) atomicAdd(P.results + cur_g, s);
+    for (int64_t b = gwarp * kWarp; b < n; b += nwarps * kWarp) {
+        const int64_t t = b + lane;
+        if (t >= n) break;
+        const uint32_t gi = P.light_list[P.list_cap - 1 - t];
+        const int64_t c = (int64_t)(gi / kWarp);
+        const int g = find_graph(P.gd, P.n_graphs, c);
+        const GraphDesc &G = P.gd[g];
+        const int x = (int)((c - G.chunk_base) * kWarp + (int64_t)(gi % kWarp));
+        const int rs = __ldg(G.rp + x);
+        const int d = __ldg(G.rp + x + 1) - rs;
+        const uint32_t h = d <= 4 ? micro_task<kPerRoot, 4>(P, G, x, rs, d)
+                                  : micro_task<kPerRoot, kMicroDeg>(P, G, x, rs, d);
+        if (!kPerRoot) {
+            if (g != cur_g) {  // a batch's next graph: this lane's hits so far go out
+                if (cur_g >= 0 && acc) atomicAdd(P.results + cur_g, acc);
                 acc = 0;
                 cur_g = g;
             }
-            if (!((mm >> lane) & 1u)) continue;
-            const int x = (int)((c - G.chunk_base) * kWarp + lane);
-            const int rs = __ldg(G.rp + x);
-            const int d = __ldg(G.rp + x + 1) - rs;
-            const uint32_t h = d <= 4 ? micro_task<kPerRoot, 4>(P, G, x, rs, d)
-                                      : micro_task<kPerRoot, kMicroDeg>(P, G, x, rs, d);
-            if (!kPerRoot) acc += h;
+            acc += h;
         }
     }
-    if (!kPerRoot) {
-        const unsigned long long s = warp_sum_u64(acc);
-        if (lane == 0 && cur_g >= 0 && s) atomicAdd(P.results + cur_g, s);
+    if (!kPerRoot) {  // one atomic per warp when its lanes ended on one graph
+        const int g0 = __reduce_max_sync(kFull, cur_g);
+        if (__all_sync(kFull, cur_g < 0 || cur_g == g0)) {
+            const unsigned long long s = warp_sum_u64(acc);
+            if (lane == 0 && g0 >= 0 && s) atomicAdd(P.results + g0, s);
+        } else if (cur_g >= 0 && acc) {
+            atomicAdd(P.results + cur_g, acc);
+        }
     }
 }
 
@@ -1215,7 +1231,7 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
     P.work = work;
     P.results = results;
     P.light_list = sc.light_list;
-    P.micro_mask = sc.micro_mask;
+    P.list_cap = total_vertices;
     P.in_cnt = sc.in_cnt;
     P.in_off = sc.in_off;
     P.in_work = sc.in_work;
@@ -1325,7 +1341,7 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
     P.work = work;
     P.results = results;
     P.light_list = sc.light_list;
-    P.micro_mask = sc.micro_mask;
+    P.list_cap = total_vertices;
     P.in_cnt = sc.in_cnt;
     P.in_off = sc.in_off;
     P.in_work = sc.in_work;

@@ -84,8 +84,8 @@ struct HeavyEntry {
 struct CountScratch {
     HeavyEntry *heavy = nullptr;  // heavy_cap entries
     int64_t heavy_cap = 0;
-    uint32_t *light_list = nullptr;         // V: light tasks, as global row index chunk * 32 + lane
-    uint32_t *micro_mask = nullptr;         // C words
+    uint32_t *light_list = nullptr;         // V: light tasks from entry 0 up, micro tasks from entry V - 1
+                                            // down, as global rows chunk * 32 + lane
     int32_t *in_cnt = nullptr;              // V
     int32_t *in_off = nullptr;              // V + 1
     unsigned long long *in_work = nullptr;  // V
@@ -93,7 +93,7 @@ struct CountScratch {
     int32_t *in_list = nullptr;             // E
     uint8_t *mid = nullptr;                 // E: edge done middle-centric
 };
-int scratch_alloc(CountScratch *sc, int64_t V, int64_t C, int64_t E, int64_t heavy_cap, cudaStream_t s);
+int scratch_alloc(CountScratch *sc, int64_t V, int64_t E, int64_t heavy_cap, cudaStream_t s);
 void scratch_free(CountScratch *sc, cudaStream_t s);
 
 // Per-launch device words, zeroed by one memset before each count.
@@ -101,11 +101,11 @@ struct CountWork {
     unsigned long long heavy_packed; // (entries << 32) | units, from the classifier
     unsigned int heavy_cursor;
     unsigned int small_cursor;       // light-task cursor
-    unsigned int aux_cursor[3];      // chunk cursors of in_count, transpose/classify, micro
+    unsigned int aux_cursor[2];      // chunk cursors of in_count, transpose/classify
     int error;
     unsigned long long total_work;   // sum over oriented edges of the cheaper side's length
-    unsigned int n_light;            // light tasks listed by the classifier
-    unsigned int pad;
+    unsigned int n_light;            // light tasks listed by the classifier (task list from the bottom)
+    unsigned int n_micro;            // micro tasks listed by the classifier (task list from the top)
 };
 
 struct Tuned {  // resolved tc_tuning with derived table geometry

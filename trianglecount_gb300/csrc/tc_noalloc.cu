@@ -35,9 +35,8 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // Byte offsets of the scratch sections (each 256-byte aligned).
 constexpr size_t kOffWork = 0;  // CountWork + 8-byte result
 constexpr size_t kOffDesc = align256(kOffWork + sizeof(CountWork) + 8);
-constexpr size_t kOffMask = align256(kOffDesc + sizeof(GraphDesc));
-constexpr size_t kOffMicro = align256(kOffMask + sizeof(uint32_t) * (kMaxRows + 1));
-constexpr size_t kOffHeavy = align256(kOffMicro + sizeof(uint32_t) * (kMaxRows / 32 + 1));
+constexpr size_t kOffTasks = align256(kOffDesc + sizeof(GraphDesc));
+constexpr size_t kOffHeavy = align256(kOffTasks + sizeof(uint32_t) * (kMaxRows + 1));
 constexpr size_t kOffInCnt = align256(kOffHeavy + sizeof(HeavyEntry) * (kMaxRows + 1));
 constexpr size_t kOffInOff = align256(kOffInCnt + sizeof(int32_t) * (kMaxRows + 1));
 constexpr size_t kOffInWork = align256(kOffInOff + sizeof(int32_t) * (kMaxRows + 2));
@@ -114,8 +113,7 @@ extern "C" int tc_count_noalloc_i32(const int32_t *d_row_ptr, const int32_t *d_c
     CountScratch sc;
     sc.heavy = (HeavyEntry *)(base + kOffHeavy);
     sc.heavy_cap = std::min(n_rows, nnz) + 1;
-    sc.light_list = (uint32_t *)(base + kOffMask);
-    sc.micro_mask = (uint32_t *)(base + kOffMicro);
+    sc.light_list = (uint32_t *)(base + kOffTasks);
     sc.in_cnt = (int32_t *)(base + kOffInCnt);
     sc.in_off = (int32_t *)(base + kOffInOff);
     sc.in_work = (unsigned long long *)(base + kOffInWork);
