@@ -263,8 +263,8 @@ struct KParams {
     int64_t heavy_cap;
     CountWork *work;
     unsigned long long *results;
-    uint32_t *light_list;  // tasks as global rows chunk * 32 + lane: work->n_light light tasks from
-                           // entry 0 up, work->n_micro micro tasks from entry list_cap - 1 down
+    uint32_t *light_list;  // tasks as global rows chunk * 32 + lane: light tasks from entry 0 up,
+                           // micro tasks from entry list_cap - 1 down (counts in work->n_tasks)
     int64_t list_cap;      // entries of light_list (the launch's rows: a row is at most one task)
     int32_t *in_cnt;       // per vertex (pooled): d+ during in_count, then middle-centric in-edges (split from in_work)
     int32_t *in_off;       // per vertex (pooled) + 1: exclusive scan of in_cnt
@@ -588,19 +588,17 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
             const bool hv = has && !micro && !light;
             const uint32_t mm = __ballot_sync(kFull, micro);
             const uint32_t lm = __ballot_sync(kFull, light);
-            if (mm) {  // list the chunk's micro tasks from the top (one atomic per chunk)
-                unsigned base = 0;
-                if (lane == 0) base = atomicAdd(&P.work->n_micro, (unsigned)__popc(mm));
+            if (mm | lm) {  // list the chunk's micro and light tasks: one atomic for both counts
+                unsigned long long base = 0;
+                if (lane == 0)
+                    base = atomicAdd(&P.work->n_tasks,
+                                     (unsigned long long)__popc(lm) | ((unsigned long long)__popc(mm) << 32));
                 base = __shfl_sync(kFull, base, 0);
+                const uint32_t below = (1u << lane) - 1u;
                 if (micro)
-                    P.light_list[P.list_cap - 1 - (int64_t)(base + __popc(mm & ((1u << lane) - 1u)))] =
+                    P.light_list[P.list_cap - 1 - (int64_t)((unsigned)(base >> 32) + __popc(mm & below))] =
                         (uint32_t)(c * kWarp + lane);
-            }
-            if (lm) {  // list the chunk's light tasks (one atomic per chunk)
-                unsigned base = 0;
-                if (lane == 0) base = atomicAdd(&P.work->n_light, (unsigned)__popc(lm));
-                base = __shfl_sync(kFull, base, 0);
-                if (light) P.light_list[base + __popc(lm & ((1u << lane) - 1u))] = (uint32_t)(c * kWarp + lane);
+                if (light) P.light_list[(unsigned)base + __popc(lm & below)] = (uint32_t)(c * kWarp + lane);
             }
             unsigned hm = __ballot_sync(kFull, hv);
             while (hm) {
@@ -711,7 +709,7 @@ __device__ __forceinline__ uint32_t micro_task(const KParams &P, const GraphDesc
 template <bool kPerRoot>
 __global__ void __launch_bounds__(kThreads) micro_kernel(KParams P) {
     const int lane = threadIdx.x & (kWarp - 1);
-    const int64_t n = P.work->n_micro;
+    const int64_t n = (int64_t)(P.work->n_tasks >> 32);
     const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
     const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / kWarp;
     unsigned long long acc = 0;  // this lane's hits for graph cur_g
@@ -1083,7 +1081,7 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
     // Warps take kLightGrab tasks at a time from the classifier's list, so the
     // last tasks of the kernel are single tasks, not whole 32-row chunks.
     int *wtab = smem + warp * (1 << P.log_warp_slots);
-    const unsigned n_light = P.work->n_light;
+    const unsigned n_light = (unsigned)P.work->n_tasks;
     for (;;) {
         unsigned t0 = 0;
         if (lane == 0) t0 = atomicAdd(&P.work->small_cursor, (unsigned)kLightGrab);

@@ -104,8 +104,9 @@ struct CountWork {
     unsigned int aux_cursor[2];      // chunk cursors of in_count, transpose/classify
     int error;
     unsigned long long total_work;   // sum over oriented edges of the cheaper side's length
-    unsigned int n_light;            // light tasks listed by the classifier (task list from the bottom)
-    unsigned int n_micro;            // micro tasks listed by the classifier (task list from the top)
+    unsigned long long n_tasks;      // tasks listed by the classifier, one atomic per chunk for both
+                                     // lists: light (low half, task list from the bottom) and micro
+                                     // (high half, from the top)
 };
 
 struct Tuned {  // resolved tc_tuning with derived table geometry
