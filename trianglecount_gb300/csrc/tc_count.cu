@@ -539,9 +539,14 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
     const unsigned long long light_max =
         min((unsigned long long)P.light_max_work,
             max((unsigned long long)kMinLight, total / (4ull * P.count_blocks * kWarpsPerBlock)));
+    // the micro / light masks of the chunks of one grab; their task-list slots
+    // are reserved with one atomic per grab (one hot word for the whole launch)
+    __shared__ uint32_t s_mask[kWarpsPerBlock][2 * kAuxGrab];
+    uint32_t *wmask = s_mask[threadIdx.x / kWarp];
     int64_t c, c_end;
     aux_next(P, 1, lane, true, c, c_end);
     for (; c < c_end; aux_next(P, 1, lane, false, c, c_end)) {
+        const int64_t c0 = c;
         for (; c < c_end; ++c) {
             const int g = find_graph(P.gd, P.n_graphs, c);
             const GraphDesc &G = P.gd[g];
@@ -588,17 +593,9 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
             const bool hv = has && !micro && !light;
             const uint32_t mm = __ballot_sync(kFull, micro);
             const uint32_t lm = __ballot_sync(kFull, light);
-            if (mm | lm) {  // list the chunk's micro and light tasks: one atomic for both counts
-                unsigned long long base = 0;
-                if (lane == 0)
-                    base = atomicAdd(&P.work->n_tasks,
-                                     (unsigned long long)__popc(lm) | ((unsigned long long)__popc(mm) << 32));
-                base = __shfl_sync(kFull, base, 0);
-                const uint32_t below = (1u << lane) - 1u;
-                if (micro)
-                    P.light_list[P.list_cap - 1 - (int64_t)((unsigned)(base >> 32) + __popc(mm & below))] =
-                        (uint32_t)(c * kWarp + lane);
-                if (light) P.light_list[(unsigned)base + __popc(lm & below)] = (uint32_t)(c * kWarp + lane);
+            if (lane == 0) {
+                wmask[2 * (c - c0)] = mm;
+                wmask[2 * (c - c0) + 1] = lm;
             }
             unsigned hm = __ballot_sync(kFull, hv);
             while (hm) {
@@ -625,6 +622,31 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
                 }
             }
         }
+        // list the grab's micro tasks (from the top) and light tasks (from the
+        // bottom): one atomic reserves both lists' slots
+        __syncwarp();
+        const int nc = (int)(c_end - c0);
+        unsigned tm = 0, tl = 0;
+        for (int k = 0; k < nc; ++k) {
+            tm += __popc(wmask[2 * k]);
+            tl += __popc(wmask[2 * k + 1]);
+        }
+        if (tm | tl) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(&P.work->n_tasks, (unsigned long long)tl | ((unsigned long long)tm << 32));
+            base = __shfl_sync(kFull, base, 0);
+            unsigned bm = (unsigned)(base >> 32), bl = (unsigned)base;
+            const uint32_t below = (1u << lane) - 1u;
+            for (int k = 0; k < nc; ++k) {
+                const uint32_t mm = wmask[2 * k], lm = wmask[2 * k + 1];
+                const uint32_t row = (uint32_t)((c0 + k) * kWarp + lane);
+                if ((mm >> lane) & 1u) P.light_list[P.list_cap - 1 - (int64_t)(bm + __popc(mm & below))] = row;
+                if ((lm >> lane) & 1u) P.light_list[bl + __popc(lm & below)] = row;
+                bm += __popc(mm);
+                bl += __popc(lm);
+            }
+        }
+        __syncwarp();  // wmask is rewritten by the next grab
     }
 }
 
