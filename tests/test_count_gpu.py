@@ -200,3 +200,34 @@ def test_flat_count_not_used_above_the_bound(tuned):
     assert got == want and st["launches"] >= 4
     with pytest.raises(tc.TCError):
         tuned.set_tuning(flat_max_deg=9)
+
+
+def test_repeated_counts_replay_a_captured_chain():
+    """From its second count a graph replays its count chain as a captured
+    CUDA graph: every replay gives the oracle's count and times the count
+    kernel; another results pointer or a tuning change re-captures, and
+    per-root counts (never captured) still agree."""
+    import torch
+    c = tc.Context(0)  # its own context: the tuning changes below stay here
+    rp, col, want = oracle.pipeline(*gen.rmat(12))
+    g = c.upload(rp, col)
+    launches = set()
+    for _ in range(4):
+        n, st = c.count(g, stats=True)
+        assert n == want
+        launches.add(st["launches"])
+        assert c.last_count_kernel_ms() > 0
+    assert len(launches) == 1  # a replay reports the captured chain's launches
+    lib = tc.lib()
+    outs = [torch.zeros(1, dtype=torch.int64, device="cuda") for _ in range(2)]
+    torch.cuda.synchronize()
+    for _ in range(2):
+        for o in outs:
+            assert lib.tc_count_async(c.handle, g.handle, o.data_ptr()) == 0
+    c.synchronize()
+    assert [int(o.item()) for o in outs] == [want, want]
+    c.set_tuning(light_max_work=512)
+    assert c.count(g) == c.count(g) == want
+    assert int(c.count_per_root(g).sum()) == want == c.count(g)
+    g.free()
+    c.close()

@@ -149,6 +149,39 @@ int ensure_count_scratch(tc_graph *g) {
     return TC_OK;
 }
 
+// Captures g's count chain (results into res) on the context's stream as a
+// CUDA graph in g->exec.  Leaves g->exec null, and the stream usable, when the
+// stream cannot be captured (the legacy or per-thread default stream, or one
+// already being captured by the caller) or the capture fails.
+void capture_count(tc_graph *g, unsigned long long *res) {
+    tc_ctx *ctx = g->ctx;
+    cudaStream_t s = ctx->stream;
+    if (s == nullptr || s == cudaStreamLegacy || s == cudaStreamPerThread) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return;
+    }
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    int nl = 0;
+    const int st = launch_count(g->d_desc, 1, (g->n_rows + 31) / 32, g->n_rows + 1, g->n_rows, g->sc, g->d_work, res,
+                                false, ctx->tuned, s, &nl, ctx->kev);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    cudaGraphExec_t exec = nullptr;
+    if (st == TC_OK && ce == cudaSuccess && graph && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+        g->exec = exec;
+        g->exec_results = res;
+        g->exec_epoch = ctx->tuning_epoch;
+        g->exec_launches = nl;
+    }
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();  // a failed capture falls back to direct launches
+}
+
 int enqueue_graph_count(tc_graph *g, unsigned long long *per_root, unsigned long long *results, int *launches) {
     tc_ctx *ctx = g->ctx;
     if (g->max_deg >= 0 && g->max_deg <= ctx->tuned.flat_max_deg) {
@@ -180,9 +213,23 @@ int enqueue_graph_count(tc_graph *g, unsigned long long *per_root, unsigned long
     }
     const int64_t chunks = (g->n_rows + 31) / 32;
     ctx->kev_recorded = chunks > 0;
-    return launch_count(g->d_desc, 1, chunks, g->n_rows + 1, g->n_rows, g->sc, g->d_work,
-                        results ? results : g->d_result, per_root != nullptr, ctx->tuned, ctx->stream, launches,
-                        ctx->kev);
+    unsigned long long *res = results ? results : g->d_result;
+    if (!per_root && chunks > 0) {
+        if (g->exec && (g->exec_results != res || g->exec_epoch != ctx->tuning_epoch)) {
+            cudaGraphExecDestroy(g->exec);
+            g->exec = nullptr;
+        }
+        if (!g->exec && g->chain_counts >= 1) capture_count(g, res);  // on failure: direct launches
+        if (g->exec) {
+            ++g->chain_counts;
+            TC_CUDA(cudaGraphLaunch(g->exec, ctx->stream));
+            if (launches) *launches = g->exec_launches;
+            return TC_OK;
+        }
+    }
+    ++g->chain_counts;
+    return launch_count(g->d_desc, 1, chunks, g->n_rows + 1, g->n_rows, g->sc, g->d_work, res, per_root != nullptr,
+                        ctx->tuned, ctx->stream, launches, ctx->kev);
 }
 
 int new_graph(tc_ctx *ctx, int64_t n_rows, int64_t nnz, int64_t n_roots, tc_graph **out) {
@@ -570,6 +617,7 @@ int tc_ctx_set_tuning(tc_ctx *c, const tc_tuning *in) {
     TC_TRY(resolve_tuning(t, c->sm_count, &r));
     c->tuning = t;
     c->tuned = r;
+    ++c->tuning_epoch;
     return TC_OK;
 }
 
@@ -678,6 +726,7 @@ int tc_graph_destroy(tc_graph *g) {
         dfree(g->rp, s);
         dfree(g->col, s);
     }
+    if (g->exec) cudaGraphExecDestroy(g->exec);
     dfree(g->d_desc, s);
     dfree(g->d_work, s);
     scratch_free(&g->sc, s);

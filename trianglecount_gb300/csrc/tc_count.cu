@@ -1239,6 +1239,17 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     return TC_OK;
 }
 
+// Records a kernel-timing event on s; inside a stream capture (the plain
+// count's cached graph) as an external event node, so that every replay of
+// the captured chain records it too.
+static int record_kernel_event(cudaEvent_t ev, cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    TC_CUDA(cudaStreamIsCapturing(s, &cs));
+    if (cs == cudaStreamCaptureStatusActive) TC_CUDA(cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal));
+    else TC_CUDA(cudaEventRecord(ev, s));
+    return TC_OK;
+}
+
 int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, int64_t total_vertices,
                  int64_t max_rows, const CountScratch &sc, CountWork *work, unsigned long long *results, bool per_root,
                  const Tuned &tn, cudaStream_t s, int *launches, cudaEvent_t *kev) {
@@ -1297,7 +1308,7 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
         TC_CUDA(cudaGetLastError());
         if (per_root) micro_kernel<true><<<aux_blocks, kThreads, 0, s>>>(P);
         else micro_kernel<false><<<aux_blocks, kThreads, 0, s>>>(P);
-        if (kev) TC_CUDA(cudaEventRecord(kev[0], s));
+        if (kev) TC_TRY(record_kernel_event(kev[0], s));
         if (bitmap) {
             const size_t bytes = (size_t)bitmap_words * 4;
             if (per_root) heavy_bitmap_kernel<true><<<tn.sm_count, kBigThreads, bytes, s>>>(P, (int)bitmap_words);
@@ -1312,7 +1323,7 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
             if (tn.hash_pairs) count_kernel<false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
             else count_kernel<false, false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
         }
-        if (kev) TC_CUDA(cudaEventRecord(kev[1], s));
+        if (kev) TC_TRY(record_kernel_event(kev[1], s));
         TC_CUDA(cudaGetLastError());
         nl += 6 + (total_vertices > 4096 ? 3 : 1);
     }

@@ -195,6 +195,7 @@ struct tc_ctx {
     int sm_count = 0;
     tc_tuning tuning{};
     tc::Tuned tuned{};
+    unsigned long long tuning_epoch = 0;  // bumped by every tuning change (cached count graphs go stale)
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t kev[2] = {nullptr, nullptr};  // around the last count kernel launch
     bool kev_recorded = false;
@@ -216,6 +217,14 @@ struct tc_graph {
     tc::CountScratch sc{};
     tc::GraphDesc desc_on_device{};  // what d_desc holds (skip re-uploads)
     bool desc_valid = false;
+    // The count chain captured as a CUDA graph on the graph's second count and
+    // replayed after that (one launch instead of ~10 stream operations), while
+    // the results pointer and the context's tuning stay the same.
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long *exec_results = nullptr;
+    unsigned long long exec_epoch = 0;
+    int exec_launches = 0;
+    int chain_counts = 0;  // chain counts enqueued so far
 };
 
 struct tc_ugraph {
