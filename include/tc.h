@@ -345,6 +345,16 @@ TC_API int tc_gen_parts_random(int64_t n, int k, uint64_t seed, int32_t *part);
 /* Contiguous assignment exactly as Halo_creation_preprocess.py:293-299:
  * l = n / k, vertices [i*l, (i+1)*l) -> part i, the last n mod k -> part 0. */
 TC_API int tc_gen_parts_contig(int64_t n, int k, int32_t *part);
+/* Balanced label-propagation parts of ug's vertices on the device, the
+ * stand-in for the reference's METIS assignment
+ * (dgl.metis_partition_assignment(G, k), Halo_creation_preprocess.py:304,
+ * 341, 378): parts of at most ceil(1.03 n / k) vertices (up to sampling
+ * noise) with few cut edges, so halos stay small.  Starts from balanced
+ * contiguous ranges; each of at most `iterations` synchronous rounds moves
+ * vertices to their neighbours' most common label, with room-limited
+ * migration.  Integer-only and seeded: the same seed gives the same parts on
+ * any GPU.  1 <= k <= 64; part is a host array of n_rows ints. */
+TC_API int tc_gen_parts_lp(tc_ctx *ctx, const tc_ugraph *ug, int k, uint64_t seed, int iterations, int32_t *part);
 
 #ifdef __cplusplus
 }

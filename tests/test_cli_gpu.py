@@ -52,6 +52,10 @@ def test_preprocess_files_match_reference_layout(prepared, tmp_path):
     for k in (2, 4, 8):
         part = F.read_node_parts(d / f"rmat13_part.csr_node_parts_random_{k}", len(rp) - 1)
         assert np.array_equal(part, gen.parts_random(len(rp) - 1, k))
+        part = F.read_node_parts(d / f"rmat13_part.csr_node_parts_contig_{k}", len(rp) - 1)
+        assert np.array_equal(part, gen.parts_contig(len(rp) - 1, k))
+        part = F.read_node_parts(d / f"rmat13_part.csr_node_parts_lp_{k}", len(rp) - 1)
+        assert part.min() >= 0 and part.max() < k and np.bincount(part).max() <= 1.05 * len(part) / k
     trp, tcol, nr, aux = F.read_tcsr(d / "rmat13.tcsr")
     assert np.array_equal(trp, orp) and np.array_equal(tcol, ocl) and aux == len(col)
 
@@ -87,3 +91,16 @@ def test_round_clean_then_wo_sort(prepared, k):
         m = re.search(r"\nTotal Vertex : (\d+) \tTotal Edges : (\d+) \tTotal Triangle : (\d+) "
                       r"\tTotal Kernel Time : \d+\.\d{4} sec\tTotal Time : \d+\.\d{6} \n\n$", out)
         assert m and int(m.group(1)) == len(rp) - 1 and int(m.group(2)) == len(col) // 2 and int(m.group(3)) == whole
+
+
+def test_round_clean_on_label_propagation_parts(prepared):
+    """The _node_parts_lp_<k> file (the stand-in for the reference's
+    _node_parts_metis_<k>) drives round_clean_sg and wo_sort_tc_256 like the
+    random parts: the parts' counts sum to the whole graph's."""
+    d, src, dst, rp, col, orp, ocl = prepared
+    k = 4
+    node_parts = d / f"rmat13_part.csr_node_parts_lp_{k}"
+    run("round_clean_sg", k, d / "rmat13_part.csr", node_parts)
+    out = run("wo_sort_tc_256", str(node_parts) + "_output.csr", k)
+    per = [int(x) for x in re.findall(r"\nPart \d+ executing :\t(\d+)\n", out)]
+    assert len(per) == k and sum(per) == oracle.count(orp, ocl)

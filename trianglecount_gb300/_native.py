@@ -118,6 +118,7 @@ _SIGS = {
     "tc_gen_chung_lu": (C.c_int, [i64, C.c_double, C.c_double, u64, vp, vp, i64]),
     "tc_gen_parts_random": (C.c_int, [i64, C.c_int, u64, vp]),
     "tc_gen_parts_contig": (C.c_int, [i64, C.c_int, vp]),
+    "tc_gen_parts_lp": (C.c_int, [vp, vp, C.c_int, u64, C.c_int, vp]),
 }
 
 _lib = None

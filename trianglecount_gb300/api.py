@@ -364,6 +364,13 @@ class Context:
         N.call("tc_graph_from_edges", self._h, _ptr(s), _ptr(d), len(s), int(n_nodes), _tie(tie), C.byref(h))
         return Graph(self, h)
 
+    def parts_lp(self, ug: UGraph, k: int, seed: int = 0x5EED1AB0, iterations: int = 20) -> np.ndarray:
+        """Balanced label-propagation parts of ug's vertices (the stand-in for
+        the reference's METIS assignment); int32 array of ug's row count."""
+        out = np.empty(ug.info()[0], np.int32)
+        N.call("tc_gen_parts_lp", self._h, ug.handle, int(k), int(seed), int(iterations), _ptr(out))
+        return out
+
     def halo_extract(self, ug: UGraph, part: np.ndarray, k: int, tie="reference") -> list[Graph]:
         p = np.ascontiguousarray(part, np.int32)
         outs = (C.c_void_p * k)()

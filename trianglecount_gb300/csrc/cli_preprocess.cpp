@@ -5,8 +5,10 @@
 //     CSR read by TC_128) and
 //   preprocess_GPU/generate_clean_undir_dataset/Halo_creation_preprocess.py
 //     (-> <name>_part.csr, the undirected CSR + degree read by round_clean_sg,
-//     and <name>_part.csr_node_parts_random_<k>, seeded here where the
-//     reference's np.random.randint is unseeded).
+//     and per k the node-parts files <name>_part.csr_node_parts_random_<k>
+//     (seeded here where the reference's np.random.randint is unseeded),
+//     _contig_<k>, and _lp_<k>: balanced label propagation on the device in
+//     place of the reference's _metis_<k> (dgl.metis_partition_assignment)).
 // Clean-up (self-loops, symmetrise, dedupe, isolated vertices) and orientation
 // run on the device.  --tcsr also writes <name>.tcsr (binary oriented CSR).
 #include <string>
@@ -91,6 +93,14 @@ int main(int argc, char **argv) {
         CLI_CHECK(tc_gen_parts_random(N, k, seed + (uint64_t)k, part.data()));
         const std::string o3 = o2 + "_node_parts_random_" + std::to_string(k);
         CLI_CHECK(tc_text_write_line(o3.c_str(), part.data(), N, 4, 'w', 1));
+        CLI_CHECK(tc_gen_parts_contig(N, k, part.data()));
+        const std::string o4 = o2 + "_node_parts_contig_" + std::to_string(k);
+        CLI_CHECK(tc_text_write_line(o4.c_str(), part.data(), N, 4, 'w', 1));
+        if (k <= 64) {
+            CLI_CHECK(tc_gen_parts_lp(ctx, ug, k, seed + (uint64_t)k, 20, part.data()));
+            const std::string o5 = o2 + "_node_parts_lp_" + std::to_string(k);
+            CLI_CHECK(tc_text_write_line(o5.c_str(), part.data(), N, 4, 'w', 1));
+        }
     }
     if (tcsr) {
         std::vector<int64_t> orp64(orp.begin(), orp.end());
