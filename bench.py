@@ -528,11 +528,29 @@ def run_parts(args, world, rank, local, pg):
                          "parts_nnz": [p.nnz for p in parts], "parts_rows": [p.n_rows for p in parts],
                          "halo_extract_s": halo_s, "sum_of_parts": int(out.sum())}
         b.free()
+    # the same graph on balanced label-propagation parts (the stand-in for the
+    # reference's METIS assignment), k = 8
+    t0 = time.perf_counter()
+    part = ctx.parts_lp(ug, 8)
+    lp_s = time.perf_counter() - t0
+    rp_u, col_u, _ = ug.download()
+    rows = np.repeat(np.arange(len(rp_u) - 1, dtype=np.int64), np.diff(rp_u))
+    cut = float((part[rows] != part[col_u]).mean())
+    del rows, rp_u, col_u
+    parts = ctx.halo_extract(ug, part, 8)
+    b = ctx.batch(parts)
+    out = b.run()
+    lp_batch_ms = _timed(stream, flush, lambda: b.run(), args.steps, args.warmup)
+    assert int(out.sum()) == whole
+    lp = {"k": 8, "partition_s": lp_s, "cut_fraction": cut, "max_part_over_mean": float(np.bincount(part).max() * 8 / V),
+          "parts_nnz": [p.nnz for p in parts], "batched_ms": lp_batch_ms, "sum_of_parts": int(out.sum())}
+    b.free()
+    del parts
     ms = per_k["8"]["batched_ms"]
     cfg = {"workload": "rmat23_ef16_halo_parts", "scale": 23, "edge_factor": 16, "V": V, "oriented_edges": E,
            "triangles": whole, "parts": per_k, "whole_graph_plain_ms": whole_ms,
            "host_generate_s": gen_s, "device_clean_s": clean_s, "device_orient_s": orient_s,
-           "partition": "seeded uniform random, k = 2, 4, 8",
+           "partition": "seeded uniform random, k = 2, 4, 8", "lp_parts_k8": lp,
            "l2": "flushed before every timed step (512 MiB memset on the launching stream)"}
     res = {"metric": METRIC, "value": world * E / (ms / 1000.0), "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
