@@ -337,6 +337,10 @@ int graph_rebind(tc_graph *g, tc_ctx *ctx) {
     tc_ctx *old = g->ctx;
     g->ctx = ctx;
     g->desc_valid = false;
+    if (g->exec) {  // the captured chain records the old context's events
+        cudaGraphExecDestroy(g->exec);
+        g->exec = nullptr;
+    }
     ctx_release(old);
     return TC_OK;
 }
