@@ -70,3 +70,22 @@ def test_upload_ugraph_rejects_asymmetric_and_self_loops(ctx):
         assert e.value.code == "TC_E_INVALID"
     ug = ctx.upload_ugraph(np.array([0, 2, 3, 4], np.int64), np.array([1, 2, 0, 0], np.int64))  # 0-1, 0-2
     assert ug.info() == (3, 4)
+
+
+@pytest.mark.parametrize("n", [1024, 2048, 1023, 1025, 3])
+@pytest.mark.parametrize("tie", ["reference", "id_asc"])
+def test_orientation_on_tile_boundaries(ctx, n, tie):
+    """Circulant graphs C_n(1, 2) have 4n undirected entries: n = 1024 and
+    2048 fill exactly one and two 4096-entry tiles, 1023 / 1025 stop just
+    short of / just past one, and n = 3 (a triangle, 6 entries) is one
+    partial warp; all vertices have the same degree, so the tie rule decides
+    every edge."""
+    i = np.arange(n, dtype=np.int64)
+    src = np.concatenate([i, i])
+    dst = np.concatenate([(i + 1) % n, (i + 2) % n])
+    rp, col = oracle.clean(src, dst)
+    ug = ctx.upload_ugraph(rp, col)
+    orp, ocl = oracle.orient(rp, col, tie)
+    drp, dcol = ctx.orient(ug, tie).download()
+    assert np.array_equal(drp, orp) and np.array_equal(dcol, ocl)
+    assert oracle.count(orp, ocl) == (1 if n == 3 else n)
