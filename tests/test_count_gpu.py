@@ -231,3 +231,31 @@ def test_repeated_counts_replay_a_captured_chain():
     assert int(c.count_per_root(g).sum()) == want == c.count(g)
     g.free()
     c.close()
+
+
+def test_repeated_counts_on_the_default_stream_and_under_a_caller_capture():
+    """The legacy default stream cannot be captured, so repeated counts there
+    launch the chain directly; a caller's own stream capture takes the chain's
+    kernels into the caller's graph (the library starts no capture of its own)."""
+    import torch
+    rp, col, want = oracle.pipeline(*gen.rmat(12))
+    c = tc.Context(0)
+    g = c.upload(rp, col)
+    c.set_stream(0)
+    assert [c.count(g) for _ in range(3)] == [want] * 3
+    s = torch.cuda.Stream()
+    c.set_stream(s.cuda_stream)
+    assert c.count(g) == want
+    out = torch.zeros(1, dtype=torch.int64, device="cuda")
+    torch.cuda.synchronize()
+    cg = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(cg, stream=s):
+        assert tc.lib().tc_count_async(c.handle, g.handle, out.data_ptr()) == 0
+    for _ in range(2):
+        out.zero_()
+        torch.cuda.synchronize()
+        cg.replay()
+        torch.cuda.synchronize()
+        assert int(out.item()) == want
+    g.free()
+    c.close()

@@ -149,19 +149,27 @@ int ensure_count_scratch(tc_graph *g) {
     return TC_OK;
 }
 
-// Captures g's count chain (results into res) on the context's stream as a
-// CUDA graph in g->exec.  Leaves g->exec null, and the stream usable, when the
-// stream cannot be captured (the legacy or per-thread default stream, or one
-// already being captured by the caller) or the capture fails.
+__global__ void set_desc_kernel(GraphDesc *dst, GraphDesc d) { *dst = d; }
+
+// A stream the library may capture: not a default stream (those cannot be
+// captured) and not one the caller is capturing (the chain's launches then
+// belong to the caller's graph).
+bool capturable(cudaStream_t s) {
+    if (s == nullptr || s == cudaStreamLegacy || s == cudaStreamPerThread) return false;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return cs == cudaStreamCaptureStatusNone;
+}
+
+// Captures g's count chain (results into res) on the context's stream, which
+// must be capturable, as a CUDA graph in g->exec.  Leaves g->exec null, and
+// the stream usable, when the capture fails.
 void capture_count(tc_graph *g, unsigned long long *res) {
     tc_ctx *ctx = g->ctx;
     cudaStream_t s = ctx->stream;
-    if (s == nullptr || s == cudaStreamLegacy || s == cudaStreamPerThread) return;
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
-        cudaGetLastError();
-        return;
-    }
     if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
         cudaGetLastError();
         return;
@@ -207,14 +215,17 @@ int enqueue_graph_count(tc_graph *g, unsigned long long *per_root, unsigned long
     d.vbase = 0;
     d.per_root = per_root;
     if (!g->desc_valid || memcmp(&d, &g->desc_on_device, sizeof(d)) != 0) {
-        TC_CUDA(cudaMemcpyAsync(g->d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, ctx->stream));
+        // a one-thread kernel with the descriptor as its parameter, not a copy
+        // from this stack frame: a caller capturing the stream keeps the value
+        set_desc_kernel<<<1, 1, 0, ctx->stream>>>(g->d_desc, d);
+        TC_CUDA(cudaGetLastError());
         g->desc_on_device = d;
         g->desc_valid = true;
     }
     const int64_t chunks = (g->n_rows + 31) / 32;
     ctx->kev_recorded = chunks > 0;
     unsigned long long *res = results ? results : g->d_result;
-    if (!per_root && chunks > 0) {
+    if (!per_root && chunks > 0 && capturable(ctx->stream)) {
         if (g->exec && (g->exec_results != res || g->exec_epoch != ctx->tuning_epoch)) {
             cudaGraphExecDestroy(g->exec);
             g->exec = nullptr;
