@@ -1337,7 +1337,7 @@ int launch_flat(const int32_t *rp, const int32_t *col, int64_t n_roots, int max_
     if (max_deg > kMicroDeg) return set_error(TC_E_INVALID, "flat count needs rows of at most %d entries", kMicroDeg);
     TC_CUDA(cudaMemsetAsync(work, 0, sizeof(CountWork), s));
     TC_CUDA(cudaMemsetAsync(result, 0, sizeof(unsigned long long), s));
-    if (kev) TC_CUDA(cudaEventRecord(kev[0], s));
+    if (kev) TC_TRY(record_kernel_event(kev[0], s));
     if (n_roots > 0) {
         const int64_t want = (n_roots + kThreads - 1) / kThreads;
         if (max_deg <= 4) {  // one resident wave, several roots per lane
@@ -1355,7 +1355,7 @@ int launch_flat(const int32_t *rp, const int32_t *col, int64_t n_roots, int max_
         }
         TC_CUDA(cudaGetLastError());
     }
-    if (kev) TC_CUDA(cudaEventRecord(kev[1], s));
+    if (kev) TC_TRY(record_kernel_event(kev[1], s));
     if (launches) *launches = n_roots > 0 ? 1 : 0;
     return TC_OK;
 }
