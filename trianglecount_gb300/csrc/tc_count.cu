@@ -727,7 +727,9 @@ __device__ __forceinline__ uint32_t micro_task(const KParams &P, const GraphDesc
 // kMicroWork) with N+(x) in registers; every streamed partner list is then at
 // most kMicroDeg long (the cheaper side), and membership is predicated
 // compares -- no hash table, no shared memory.  Tasks with d+(x) <= 4 (most
-// of a road network's) take a 4-wide path: a quarter of the compares.
+// of a road network's) take a 4-wide path: a quarter of the compares.  Warps
+// take 32 consecutive tasks from the top of the task list, so every lane has
+// one (a chunk of 32 rows holds only a few micro tasks on most graphs).
 template <bool kPerRoot>
 __global__ void __launch_bounds__(kThreads) micro_kernel(KParams P) {
     const int lane = threadIdx.x & (kWarp - 1);
