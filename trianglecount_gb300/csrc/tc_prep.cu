@@ -511,8 +511,8 @@ __global__ void halo_rows_kernel(const int32_t *__restrict__ rp, const int2 *__r
 
 // Pass 2 (strided): ranks each tile's P and H entries again from the stored
 // bits with warp ballots and writes every local edge at lrp[local row] + its
-// offset (lcol = the local id of the target, lrow = the local row, for the
-// prune's compaction); consecutive lanes write consecutive positions.
+// offset (lcol = the local id of the target); consecutive lanes write
+// consecutive positions.
 __global__ void __launch_bounds__(kOT) halo_tile_write_kernel(const int32_t *__restrict__ rowid,
                                                                const int32_t *__restrict__ col,
                                                                const int2 *__restrict__ ld,
@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(kOT) halo_tile_write_kernel(const int32_t *__r
                                                                const int32_t *__restrict__ lrp,
                                                                const int32_t *__restrict__ base_p,
                                                                const int32_t *__restrict__ base_h,
-                                                               int32_t *__restrict__ lcol, int32_t *__restrict__ lrow) {
+                                                               int32_t *__restrict__ lcol) {
     const int64_t j0 = strided_first();
     const int lane = threadIdx.x & 31;
     const uint32_t cw = bits[(int64_t)blockIdx.x * kOT + threadIdx.x];  // pass 1's run of this lane
@@ -546,7 +546,6 @@ __global__ void __launch_bounds__(kOT) halo_tile_write_kernel(const int32_t *__r
             const int lr = __ldg(lrp + ls);
             const int o = kp ? lr - __ldg(base_p + s) + pr + __popc(bp & lt) : lr - __ldg(base_h + s) + hr + __popc(bh & lt);
             lcol[o] = __ldg(ld + __ldg(col + j)).x;
-            lrow[o] = ls;
         }
         pr += __popc(bp);
         hr += __popc(bh);
@@ -611,11 +610,18 @@ __global__ void prune_rows_kernel(const uint8_t *alive, const int32_t *nid, cons
     }
 }
 
-__global__ void prune_cols_kernel(const int32_t *lrow, const int32_t *lcol, const int32_t *lrp, int64_t nnz,
-                                  const uint8_t *alive, const int32_t *nid, const int32_t *newpos, int32_t *col2) {
-    GRID_STRIDE(e, nnz) {
-        const int i = lrow[e];
-        if (alive[i]) col2[newpos[i] + (int)(e - lrp[i])] = nid[lcol[e]];
+// One warp per surviving local row: its entries, renumbered, at the row's new
+// start (consecutive lanes write consecutive positions).
+__global__ void prune_cols_kernel(const int32_t *__restrict__ lcol, const int32_t *__restrict__ lrp, int64_t n,
+                                  const uint8_t *__restrict__ alive, const int32_t *__restrict__ nid,
+                                  const int32_t *__restrict__ newpos, int32_t *__restrict__ col2) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = w0; i < n; i += nw) {
+        if (!alive[i]) continue;
+        const int a = lrp[i], b = lrp[i + 1], o = newpos[i] - a;
+        for (int e = a + lane; e < b; e += 32) col2[o + e] = nid[lcol[e]];
     }
 }
 
@@ -962,14 +968,12 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
         TC_TRY(scan_exclusive_i32(cnt.p, lrp.p, n_comb, s));
         int32_t lnnz = 0;
         TC_TRY(d2h_scalar(&lnnz, lrp.p + n_comb, s));
-        DBuf<int32_t> lcol, lrow, front, next, fn;
+        DBuf<int32_t> lcol, front, next, fn;
         DBuf<uint8_t> removed;
         TC_TRY(lcol.alloc((size_t)lnnz, s));
-        TC_TRY(lrow.alloc((size_t)lnnz, s));
         if (tiles && lnnz)
             halo_tile_write_kernel<<<(unsigned)tiles, kOT, 0, s>>>(ug->rowid, ug->col, ld.p, bits.p, nnz, tiles,
-                                                                    tile_off.p, lrp.p, base_p.p, base_h.p, lcol.p,
-                                                                    lrow.p);
+                                                                    tile_off.p, lrp.p, base_p.p, base_h.p, lcol.p);
         TC_CUDA(cudaGetLastError());
         // prune: peel halo vertices of zero in-degree until none is left
         TC_TRY(removed.alloc((size_t)std::max<int64_t>(n_comb, 1), s));
@@ -1026,8 +1030,8 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
             prune_rows_kernel<<<grid(n_comb, ctx), 256, 0, s>>>(alive.p, nid.p, newpos.p, n_comb, rp2.p);
             TC_CUDA(cudaMemcpyAsync(rp2.p + nl, &nn, sizeof(int32_t), cudaMemcpyHostToDevice, s));
             if (lnnz)
-                prune_cols_kernel<<<grid(lnnz, ctx), 256, 0, s>>>(lrow.p, lcol.p, lrp.p, lnnz, alive.p, nid.p, newpos.p,
-                                                                  col2.p);
+                prune_cols_kernel<<<grid(n_comb * 32, ctx), 256, 0, s>>>(lcol.p, lrp.p, n_comb, alive.p, nid.p,
+                                                                         newpos.p, col2.p);
             TC_CUDA(cudaGetLastError());
             TC_CUDA(cudaStreamSynchronize(s));
             out_rp = rp2.release();
