@@ -58,7 +58,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["rmat21", "road", "rmat16", "rmat18", "rmat23", "rmat23_parts", "batch256",
-                                           "refstudy",
+                                           "refstudy", "io",
                                            "serve"], default="rmat21")
     ap.add_argument("--rates", default="50,200,1000,4000", help="serve: Poisson arrival rates (requests/s)")
     ap.add_argument("--requests", type=int, default=400, help="serve: requests per rate")
@@ -694,6 +694,71 @@ def run_serve(args, world, rank, local, pg):
     return res
 
 
+def run_io(args, world, rank, local, pg):
+    """The TC_128 driver's host path (its time goes to reading the .csr text):
+    R-MAT 21's oriented CSR written as a .csr file, read by the reference's
+    one-fscanf-per-integer loop (restated in the oracle, one thread) and by the
+    library's parallel text parser, and written and read back as the binary
+    .tcsr.  Host work only; rank 0 runs it."""
+    import shutil
+    import tempfile
+
+    import oracle
+    import trianglecount_gb300 as tc
+    from trianglecount_gb300 import formats as F
+    from trianglecount_gb300 import generators as gen
+    if rank != 0:
+        return None
+    with tc.Context(local) as ctx:
+        g = ctx.graph_from_edges(*gen.rmat(21, 16))
+        rp, col = g.download()
+        g.free()
+    V, E = len(rp) - 1, len(col)
+    d = tempfile.mkdtemp(prefix="tc_io_")
+    try:
+        text = os.path.join(d, "rmat21_output.csr")
+        F.write_csr(text, V, 2 * E, rp, col)
+        text_bytes = os.path.getsize(text)
+        n_ints = 4 + (V + 1) + E
+        t0 = time.perf_counter()
+        hdr, r1, c1 = oracle.read_csr_fscanf(text)
+        fscanf_s = time.perf_counter() - t0
+        assert np.array_equal(r1, rp) and np.array_equal(c1, col)
+        del r1, c1
+        parse_s = []
+        for _ in range(max(3, args.steps)):
+            t0 = time.perf_counter()
+            fast = F.read_csr(text)
+            parse_s.append(time.perf_counter() - t0)
+        assert np.array_equal(fast.row_ptr, rp) and np.array_equal(fast.col, col)
+        del fast
+        bin_path = os.path.join(d, "rmat21.tcsr")
+        t0 = time.perf_counter()
+        F.write_tcsr(bin_path, rp, col)
+        tcsr_write_s = time.perf_counter() - t0
+        tcsr_read_s = []
+        for _ in range(max(3, args.steps)):
+            t0 = time.perf_counter()
+            r2, c2, _, _ = F.read_tcsr(bin_path)
+            tcsr_read_s.append(time.perf_counter() - t0)
+        assert np.array_equal(r2, rp) and np.array_equal(c2, col)
+        tcsr_bytes = os.path.getsize(bin_path)
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    parse = statistics.median(parse_s)
+    cfg = {"workload": "rmat21_csr_text_io", "V": V, "oriented_edges": E, "text_bytes": text_bytes,
+           "integers": n_ints, "fscanf_s": fscanf_s, "parallel_parse_s": parse,
+           "parallel_parse_gbs": text_bytes / parse / 1e9, "speedup_vs_fscanf": fscanf_s / parse,
+           "tcsr_bytes": tcsr_bytes, "tcsr_write_s": tcsr_write_s, "tcsr_read_s": statistics.median(tcsr_read_s),
+           "host_threads": os.cpu_count(), "note": "host work; files on the local disk (page cache warm after the write)"}
+    return {"metric": "integers parsed/s", "value": n_ints / parse, "unit": "integers/s", "n_gpus": world,
+            "steps": max(3, args.steps), "warmup": 0, "ms_per_step": parse * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded R-MAT 21)",
+            "config": cfg,
+            "cpu_baseline": {"value": n_ints / fscanf_s, "unit": "integers/s", "cores": 1, "kind": "port",
+                             "sample": "the whole file, the reference's fscanf loop (one thread)"}}
+
+
 def main():
     args = parse()
     world, rank, local, pg = dist_setup(args)
@@ -701,9 +766,9 @@ def main():
         run_reference(args, world, rank)
     else:
         fn = {"rmat23_parts": run_parts, "batch256": run_batch, "serve": run_serve,
-              "refstudy": run_refstudy}.get(args.workload, run_ours)
+              "refstudy": run_refstudy, "io": run_io}.get(args.workload, run_ours)
         res = fn(args, world, rank, local, pg)
-        if rank == 0:
+        if rank == 0 and res is not None:
             print(json.dumps(res), flush=True)
     if pg is not None:
         pg.destroy_process_group()

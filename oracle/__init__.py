@@ -55,6 +55,10 @@ def lib() -> C.CDLL:
         L.orc_halo_part.argtypes = [i64, vp, vp, vp, vp, i64, C.c_int, vp, vp, C.POINTER(i64), C.POINTER(i64)]
         L.orc_num_threads.restype = C.c_int
         L.orc_num_threads.argtypes = []
+        L.orc_read_csr_fscanf.restype = C.c_int
+        L.orc_read_csr_fscanf.argtypes = [C.c_char_p, vp, C.POINTER(C.POINTER(C.c_int32)), C.POINTER(C.POINTER(C.c_int32))]
+        L.orc_free.restype = None
+        L.orc_free.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -208,3 +212,20 @@ def ref_tc128(row_ptr, col, runs: int = 1):
     if rc != 0:
         raise RuntimeError(f"reference kernel launch failed: {err.value.decode()}")
     return out[:V], ms.value
+
+
+def read_csr_fscanf(path):
+    """The TC_128 driver's .csr reader restated (one fscanf per integer,
+    ShareKernelTCV62_update_v1.cu:206-230): (header[4], row_ptr, col)."""
+    L = lib()
+    hdr = np.zeros(4, np.int64)
+    rp, cl = C.POINTER(C.c_int32)(), C.POINTER(C.c_int32)()
+    if L.orc_read_csr_fscanf(os.fsencode(path), hdr.ctypes.data_as(C.c_void_p), C.byref(rp), C.byref(cl)) != 0:
+        raise OSError(f"cannot read {path}")
+    try:
+        row_ptr = np.ctypeslib.as_array(rp, shape=(int(hdr[2]),)).copy() if hdr[2] else np.zeros(0, np.int32)
+        col = np.ctypeslib.as_array(cl, shape=(int(hdr[3]),)).copy() if hdr[3] else np.zeros(0, np.int32)
+    finally:
+        L.orc_free(C.cast(rp, C.c_void_p))
+        L.orc_free(C.cast(cl, C.c_void_p))
+    return hdr, row_ptr, col

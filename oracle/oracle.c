@@ -20,6 +20,10 @@
  *                    per-block g_sum; src/WithPartition/without_sorting_tc.cu:57-219
  *                    with roots 0..t_ver-1), as an OpenMP merge intersection
  *   orc_count_brute  independent O(sum d^2) count on the undirected graph
+ *   orc_read_csr_fscanf  the TC_128 driver's .csr reader: one fscanf("%d")
+ *                    per integer, single-threaded
+ *                    (src/WithoutPartition/ShareKernelTCV62_update_v1.cu:206-230),
+ *                    the CPU baseline of the library's parallel text parser
  *   orc_halo_part    per-part halo subgraph
  *                    (preprocess_GPU/Halo_cleanned_preprocess/round_clean_subgraph.cu:357-902)
  *                    with the prune loop of
@@ -31,6 +35,7 @@
  * edge exactly once, so the count is the same; the files differ.
  */
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -413,3 +418,47 @@ int64_t orc_halo_part(int64_t V, const int64_t *row_ptr, const int64_t *col, con
     free(stack);
     return op;
 }
+
+/* The .csr reader of the TC_128 driver
+ * (src/WithoutPartition/ShareKernelTCV62_update_v1.cu:206-230): the header
+ * "V E row_ptr_s col_idx_s", then row_ptr_s and col_idx_s integers, each read
+ * by its own fscanf("%d").  hdr gets the four header values; *row_ptr and *col
+ * are malloc'd (release with orc_free).  Returns 0, or -1 when the file cannot
+ * be opened or ends early. */
+int orc_read_csr_fscanf(const char *path, int64_t hdr[4], int32_t **row_ptr, int32_t **col)
+{
+    FILE *f = fopen(path, "r");
+    int v[4], d;
+    int32_t *rp = NULL, *cl = NULL;
+    *row_ptr = NULL;
+    *col = NULL;
+    if (!f) return -1;
+    for (int i = 0; i < 4; ++i)
+        if (fscanf(f, "%d", &v[i]) != 1 || v[i] < 0) {
+            fclose(f);
+            return -1;
+        }
+    rp = (int32_t *)malloc(sizeof(int32_t) * (size_t)(v[2] ? v[2] : 1));
+    cl = (int32_t *)malloc(sizeof(int32_t) * (size_t)(v[3] ? v[3] : 1));
+    for (int i = 0; rp && cl && i < v[2]; ++i) {
+        if (fscanf(f, "%d", &d) != 1) goto fail;
+        rp[i] = d;
+    }
+    for (int j = 0; rp && cl && j < v[3]; ++j) {
+        if (fscanf(f, "%d", &d) != 1) goto fail;
+        cl[j] = d;
+    }
+    if (!rp || !cl) goto fail;
+    fclose(f);
+    for (int i = 0; i < 4; ++i) hdr[i] = v[i];
+    *row_ptr = rp;
+    *col = cl;
+    return 0;
+fail:
+    fclose(f);
+    free(rp);
+    free(cl);
+    return -1;
+}
+
+void orc_free(void *p) { free(p); }

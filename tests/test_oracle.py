@@ -144,3 +144,20 @@ def test_fullsize_generators_are_pinned(golden_dir):
     for name, make in (("rmat21", lambda: gen.rmat(21, 16)), ("road", gen.road), ("rmat23", lambda: gen.rmat(23, 16))):
         src, dst = make()
         assert int((src * 1000003 + dst).sum() % (1 << 61)) == full[name]["edge_checksum"], name
+
+
+def test_fscanf_reader_matches_parallel_parser(tmp_path):
+    """The TC_128 driver's one-fscanf-per-integer reader (restated in the
+    oracle) and the library's parallel text parser read the same .csr."""
+    from trianglecount_gb300 import formats as F
+    rp, col, _ = oracle.pipeline(*gen.rmat(11))
+    p = tmp_path / "g_output.csr"
+    F.write_csr(p, len(rp) - 1, 2 * len(col), rp, col)
+    hdr, r1, c1 = oracle.read_csr_fscanf(p)
+    fast = F.read_csr(p)
+    assert list(hdr) == [len(rp) - 1, 2 * len(col), len(rp), len(col)] == [fast.V, fast.E, len(fast.row_ptr), len(fast.col)]
+    assert np.array_equal(r1, rp) and np.array_equal(fast.row_ptr, rp)
+    assert np.array_equal(c1, col) and np.array_equal(fast.col, col)
+    p.write_text(p.read_text()[: len(p.read_text()) // 2])  # ends early
+    with pytest.raises(OSError):
+        oracle.read_csr_fscanf(p)
