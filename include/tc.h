@@ -167,9 +167,11 @@ TC_API int tc_count(tc_ctx *ctx, tc_graph *g, uint64_t *out, tc_count_stats *sta
 /* Enqueue the count of g on the context stream; the result lands in the
  * 8-byte device word d_out (overwritten).  Returns without synchronising.
  * From a graph's second count on (tc_count or tc_count_async), its launch
- * chain is captured once as a CUDA graph and replayed: one launch per count,
- * re-captured when d_out or the context's tuning changes.  A stream that the
- * caller is capturing, or a default stream, gets the plain launches. */
+ * chain is captured once as a CUDA graph and replayed: one launch per count.
+ * It is re-captured when the context's tuning changes, and for a new d_out
+ * once two counts in a row used it (a d_out that changes every call gets
+ * the plain launches).  A stream that the caller is capturing, or a default
+ * stream, gets the plain launches. */
 TC_API int tc_count_async(tc_ctx *ctx, tc_graph *g, uint64_t *d_out);
 /* Per-root counts, the reference's g_sum[u] (ShareKernelTCV62_update_v1.cu:175-186):
  * per_root[u] for u in [0, n_roots), host array. */

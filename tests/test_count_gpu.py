@@ -205,8 +205,9 @@ def test_flat_count_not_used_above_the_bound(tuned):
 def test_repeated_counts_replay_a_captured_chain():
     """From its second count a graph replays its count chain as a captured
     CUDA graph: every replay gives the oracle's count and times the count
-    kernel; another results pointer or a tuning change re-captures, and
-    per-root counts (never captured) still agree."""
+    kernel; results pointers that change every call are counted directly, a
+    pointer used twice in a row or a tuning change re-captures, and per-root
+    counts (never captured) still agree."""
     import torch
     c = tc.Context(0)  # its own context: the tuning changes below stay here
     rp, col, want = oracle.pipeline(*gen.rmat(12))
@@ -222,10 +223,16 @@ def test_repeated_counts_replay_a_captured_chain():
     outs = [torch.zeros(1, dtype=torch.int64, device="cuda") for _ in range(2)]
     torch.cuda.synchronize()
     for _ in range(2):
-        for o in outs:
+        for o in outs:  # a pointer that changes every call: direct launches
             assert lib.tc_count_async(c.handle, g.handle, o.data_ptr()) == 0
     c.synchronize()
     assert [int(o.item()) for o in outs] == [want, want]
+    for _ in range(3):  # the same pointer twice in a row: captured, then replayed
+        outs[0].zero_()
+        torch.cuda.synchronize()
+        assert lib.tc_count_async(c.handle, g.handle, outs[0].data_ptr()) == 0
+        c.synchronize()
+        assert int(outs[0].item()) == want
     c.set_tuning(light_max_work=512)
     assert c.count(g) == c.count(g) == want
     assert int(c.count_per_root(g).sum()) == want == c.count(g)

@@ -227,11 +227,18 @@ int prepare_graph_count(tc_graph *g, unsigned long long *per_root, unsigned long
     }
     unsigned long long *res = results ? results : g->d_result;
     if (!per_root && g->n_rows > 0 && capturable(ctx->stream)) {
-        if (g->exec && (g->exec_results != res || g->exec_epoch != ctx->tuning_epoch)) {
+        if (g->exec && g->exec_epoch != ctx->tuning_epoch) {
             cudaGraphExecDestroy(g->exec);
             g->exec = nullptr;
         }
-        if (!g->exec && g->chain_counts >= 1) capture_count(g, res);  // on failure: direct launches
+        // (re)capture for a results pointer that the previous count used too;
+        // a pointer seen once is counted with direct launches
+        const bool stable = g->chain_counts >= 1 && res == g->last_results;
+        if (stable && g->exec && g->exec_results != res) {
+            cudaGraphExecDestroy(g->exec);
+            g->exec = nullptr;
+        }
+        if (stable && !g->exec) capture_count(g, res);  // on failure: direct launches
     }
     return TC_OK;
 }
@@ -248,6 +255,7 @@ int enqueue_graph_count(tc_graph *g, unsigned long long *per_root, unsigned long
     const int64_t chunks = (g->n_rows + 31) / 32;
     ctx->kev_recorded = chunks > 0;
     ++g->chain_counts;
+    if (!per_root) g->last_results = res;
     if (!per_root && g->exec && g->exec_results == res && g->exec_epoch == ctx->tuning_epoch &&
         capturable(ctx->stream)) {
         TC_CUDA(cudaGraphLaunch(g->exec, ctx->stream));

@@ -219,9 +219,11 @@ struct tc_graph {
     bool desc_valid = false;
     // The count chain captured as a CUDA graph on the graph's second count and
     // replayed after that (one launch instead of ~10 stream operations), while
-    // the results pointer and the context's tuning stay the same.
+    // the results pointer and the context's tuning stay the same; a results
+    // pointer is captured once two counts in a row used it.
     cudaGraphExec_t exec = nullptr;
     unsigned long long *exec_results = nullptr;
+    unsigned long long *last_results = nullptr;  // results pointer of the previous chain count
     unsigned long long exec_epoch = 0;
     int exec_launches = 0;
     int chain_counts = 0;  // chain counts enqueued so far
