@@ -1,31 +1,41 @@
 """Benchmark: exact triangle counting throughput (oriented edges/s) on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload rmat21|road|rmat16|rmat18|rmat23|rmat23_parts|batch256|serve|refstudy]
+                    [--workload rmat23_parts|rmat21|road|rmat16|rmat18|rmat23|rmat23_k8_batch|
+                                batch256|serve|refstudy|io]
 
-One step = one exact count of the workload graph (classify + persistent count
-kernel, or the one flat kernel for a graph with no row longer than 8; result
-in device memory).  Default workload: R-MAT scale 21, edge
-factor 16, (a, b, c) = (0.57, 0.19, 0.19), seeded and vertex-permuted,
-cleaned and degree-oriented on the device (the plain TC_128 path on the
-"two shapes on one GB300" configuration, shape a).
+Default workload (rmat23_parts): the partitioned halo path on R-MAT scale 23,
+edge factor 16, (a, b, c) = (0.57, 0.19, 0.19), seeded and vertex-permuted,
+cleaned and degree-oriented on the device; k = 2, 4, 8 seeded random parts,
+halo subgraphs extracted on the device.  One step = one count of all k = 8
+parts in one batched persistent launch (CUDA-graph replay, counting halo:
+TC_HALO_COUNT); beside it, per part: one launch per part with a host sync
+after each (the reference's per-part loop, without_sorting_tc.cu:244-465) on
+the reference's parts and on the counting parts, and the unpartitioned count.
+Every result is checked: the parts sum to the whole graph's count.
 
 Printed on rank 0 as ONE JSON line:
-  value      whole-job oriented edges/s with the graph resident in HBM, L2
-             flushed (512 MiB memset) before every timed step, CUDA events on
-             the launching stream, max over ranks
-  e2e        the same metric through the C ABI (tc_count_csr_i32) from pinned
-             host buffers: upload + validation + count + result read-back
-  roofline   algorithmic bytes of the count per launch
-             B = 4(V+1) + 12|E+| + 4 W+ + 8 (W+ = sum over oriented edges of
-             d+(v)) / kernel time, against the measured HBM copy peak
-  cpu_baseline  the OpenMP merge-intersection oracle on the machine's host cores
+  value      whole-job oriented edges/s (|E+| of the graph / batched k = 8 time)
+             with the parts resident in HBM, L2 flushed (512 MiB memset)
+             before every timed step, CUDA events on the launching stream,
+             max over ranks
+  e2e        the same metric through the C ABI (tc_count_parts_csr_i32) from
+             pinned host buffers of the k = 8 parts: upload + validation +
+             batched count + result read-back
+  roofline   of the dominant kernel (count_kernel of the batched launch):
+             achieved = the bytes this design must read (each root list, each
+             edge's row_ptr pair and the cheaper side's list) / its device time;
+             the DRAM traffic of one launch (ncu) and the fixed per-edge model
+             of the survey (every N+(v) read) beside it
+  cpu_baseline  the OpenMP merge-intersection oracle on the machine's host cores,
+             one full count of the graph
   reference_gpu_kernel  the reference's own TC_128 kernel (built from its
-             sources for sm_103a) on the same graph and GPU, when available
+             sources for sm_103a) on the unpartitioned graph, same GPU
 
---impl reference times the reference's CPU path on the host cores: the
-OpenMP oracle restatement (the reference's counting code is CUDA only; its
-CPU orientation tool has no counter), one bounded sample of roots per step.
+--impl reference times the reference's CPU path on the host cores: the OpenMP
+oracle restatement (the reference's counting code is CUDA only; its CPU
+orientation tool has no counter), one bounded slice of roots per step; its
+input comes from the oracle's own generators (no library code is loaded).
 """
 from __future__ import annotations
 
@@ -57,9 +67,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["rmat21", "road", "rmat16", "rmat18", "rmat23", "rmat23_parts", "batch256",
-                                           "refstudy", "io",
-                                           "serve"], default="rmat21")
+    ap.add_argument("--workload", choices=["rmat23_parts", "rmat21", "road", "rmat16", "rmat18", "rmat23",
+                                           "rmat23_k8_batch", "batch256", "refstudy", "io", "serve"],
+                    default="rmat23_parts")
+    ap.add_argument("--scale", type=int, default=23,
+                    help="rmat23_parts / rmat23_k8_batch: R-MAT scale (23 is the benchmark; smaller for tests)")
     ap.add_argument("--rates", default="50,200,1000,4000", help="serve: Poisson arrival rates (requests/s)")
     ap.add_argument("--requests", type=int, default=400, help="serve: requests per rate")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
@@ -166,13 +178,40 @@ def barrier(pg):
         pg.barrier()
 
 
+def parts_config(scale: int) -> dict:
+    """The partitioned workload as both arms name it."""
+    return {"workload": f"rmat{scale}_ef16_halo_parts", "generator": "R-MAT", "scale": scale, "edge_factor": 16,
+            "abc": [0.57, 0.19, 0.19], "seed": 0x5EED0000 + scale if scale not in (16, 21, 23) else
+            {16: 0x5EED0016, 21: 0x5EED0021, 23: 0x5EED0023}[scale], "vertex_permutation": True,
+            "parts_k": [2, 4, 8], "partition": "seeded uniform random parts (seed 0x5EED9A27 + k)",
+            "headline": "k = 8 parts (counting halo) in one batched persistent launch",
+            "tie_break": "reference (deg u < deg w, or equal and w < u)", "index_type": "int32",
+            "l2": "flushed before every timed step (512 MiB memset on the launching stream)"}
+
+
 def run_reference(args, world, rank):
-    """CPU path of the reference (OpenMP oracle restatement), rank 0 only."""
+    """CPU path of the reference (OpenMP oracle restatement), rank 0 only.
+    R-MAT inputs come from the oracle's own generators, so this arm loads no
+    library code."""
     if rank != 0:
         return
     import oracle
-    src, dst, cfg = workload_edges(args.workload)
-    orp, ocl, _ = oracle.pipeline(src, dst)
+    if args.workload in ("rmat23_parts", "rmat23_k8_batch"):
+        cfg = parts_config(args.scale)
+        src, dst = oracle.gen_rmat(args.scale)
+    elif args.workload.startswith("rmat"):
+        scale = int("".join(ch for ch in args.workload[4:6] if ch.isdigit()))
+        src, dst = oracle.gen_rmat(scale)
+        cfg = {"workload": f"rmat{scale}_ef16_plain", "generator": "R-MAT", "scale": scale, "edge_factor": 16,
+               "abc": list(oracle.RMAT_ABC), "seed": oracle.SEED_RMAT.get(scale, 0x5EED0000 + scale),
+               "vertex_permutation": True}
+    else:
+        src, dst, cfg = workload_edges(args.workload)
+    rp, col = oracle.clean(src, dst)
+    del src, dst
+    orp, ocl = oracle.orient(rp, col)
+    del rp, col
+    orp, ocl = orp.astype(np.int32), ocl.astype(np.int32)
     V = len(orp) - 1
     n_samples = 8
     bounds = [V * i // n_samples for i in range(n_samples + 1)]
@@ -192,11 +231,12 @@ def run_reference(args, world, rank):
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic", "config": cfg,
+        "higher_is_better": True, "scaling": "strong" if "halo_parts" in cfg["workload"] else "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic", "config": cfg,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"one 1/{n_samples} slice of the roots per step (permuted ids), "
-                                   "OpenMP merge intersection, schedule(dynamic,64)"},
+                                   "OpenMP merge intersection, schedule(dynamic,64); the parts of the graph "
+                                   "sum to its whole count, so the whole graph's roots are the sample space"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -485,78 +525,300 @@ def run_refstudy(args, world, rank, local, pg):
     return res
 
 
+def _part_bytes(prp: np.ndarray, pcol: np.ndarray, n_roots: int) -> tuple[int, int, int]:
+    """Bytes one count of a graph (roots [0, n_roots)) reads: (model, min-side, W+).
+    model = 4(R+1) + 12 E_R + 4 W+ + 8: the roots' row_ptr and lists, each
+    root edge u -> v's row_ptr pair and all of N+(v) (W+ = sum d+(v));
+    min-side: the same with min(d+(u), d+(v)) entries per edge, the list of
+    the cheaper side, which is what this design streams through a hash."""
+    d = np.diff(prp).astype(np.int64)
+    er = int(prp[n_roots])
+    if er == 0:
+        return 4 * (n_roots + 1) + 8, 4 * (n_roots + 1) + 8, 0
+    du = np.repeat(d[:n_roots], d[:n_roots])
+    dv = d[pcol[:er]]
+    W = int(dv.sum())
+    P = int(np.minimum(du, dv).sum())
+    base = 4 * (n_roots + 1) + 12 * er + 8
+    return base + 4 * W, base + 4 * P, W
+
+
 def run_parts(args, world, rank, local, pg):
-    """Partitioned halo path on R-MAT scale 23: device clean-up, orientation and
-    halo extraction for k = 2, 4, 8 seeded random parts; every part counted by
-    its own launch (host sync after each, as the reference's per-part loop)
-    versus all parts in one persistent launch (CUDA-graph replay)."""
+    """Partitioned halo path (the default workload): device clean-up,
+    orientation and halo extraction of R-MAT scale 23 for k = 2, 4, 8 seeded
+    random parts, in the reference's halo (round_clean_sg's parts) and the
+    counting halo (TC_HALO_COUNT); per-part launches with a host sync after
+    each (the reference's loop, without_sorting_tc.cu:244-465) versus one
+    batched persistent launch; the unpartitioned count beside them.  With
+    N > 1 ranks, the k = 8 counting parts are split over the ranks by work
+    (largest first), each rank counts its parts in one batched launch, and the
+    per-part counts are summed: a fixed total, so scaling is strong."""
+    import ctypes as C
+
     import torch
 
     import trianglecount_gb300 as tc
     from trianglecount_gb300 import generators as gen
+    from trianglecount_gb300 import shard
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     ctx = tc.Context(local)
     ctx.set_stream(stream.cuda_stream)
+    lib = tc.lib()
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    scale = args.scale
+    cfg = parts_config(scale)
+    detail: dict = {}
+
     t0 = time.perf_counter()
-    src, dst = gen.rmat(23, 16)
-    gen_s = time.perf_counter() - t0
-    torch.cuda.synchronize()
+    src, dst = gen.rmat(scale, 16)
+    detail["host_generate_s"] = time.perf_counter() - t0
     t0 = time.perf_counter()
     ug = ctx.ugraph_from_edges(src, dst)
-    clean_s = time.perf_counter() - t0
-    t0 = time.perf_counter()
+    ctx.synchronize()
+    detail["device_clean_s"] = time.perf_counter() - t0
+    del src, dst
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
     og = ctx.orient(ug)
-    orient_s = time.perf_counter() - t0
+    e1.record(stream)
+    e1.synchronize()
+    detail["device_orient_ms"] = e0.elapsed_time(e1)
     V, E = og.n_rows, og.nnz
+    rp, col = og.download()
+    cfg.update({"V": V, "oriented_edges": E})
     whole = ctx.count(og)
-    whole_ms = _timed(stream, flush, lambda: ctx.count(og), args.steps, args.warmup)
-    per_k = {}
-    for k in (2, 4, 8):
-        part = gen.parts_random(V, k)
-        t0 = time.perf_counter()
-        parts = ctx.halo_extract(ug, part, k)
-        halo_s = time.perf_counter() - t0
-        plain_ms = _timed(stream, flush, lambda: ctx.count_each(parts), args.steps, args.warmup)
-        b = ctx.batch(parts)
-        out = b.run()
-        batch_ms = _timed(stream, flush, lambda: b.run(), args.steps, args.warmup)
-        assert int(out.sum()) == whole and int(ctx.count_each(parts).sum()) == whole
-        per_k[str(k)] = {"plain_per_part_ms": plain_ms, "batched_ms": batch_ms, "speedup": plain_ms / batch_ms,
-                         "parts_nnz": [p.nnz for p in parts], "parts_rows": [p.n_rows for p in parts],
-                         "halo_extract_s": halo_s, "sum_of_parts": int(out.sum())}
+    detail["triangles"] = whole
+
+    def timed(fn, after=None):
+        ms, extra = [], []
+        for i in range(args.warmup + args.steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                a.record(stream)
+            fn()
+            with torch.cuda.stream(stream):
+                b.record(stream)
+            b.synchronize()
+            if i >= args.warmup:
+                ms.append(a.elapsed_time(b))
+                if after is not None:
+                    extra.append(after())
+        return ms, extra
+
+    def mean(x):
+        return sum(x) / len(x) if x else 0.0
+
+    clocks = ClockSampler(local)
+    per_k, head = {}, None
+    if world == 1:
+        clocks.start()
+        d_out = torch.zeros(1, dtype=torch.int64, device=dev)
+        kms = C.c_float()
+
+        def kernel_ms():
+            lib.tc_ctx_last_count_kernel_ms(ctx.handle, C.byref(kms))
+            return kms.value
+
+        w_ms, w_k = timed(lambda: lib.tc_count_async(ctx.handle, og.handle, d_out.data_ptr()), kernel_ms)
+        assert int(d_out.item()) == whole
+        detail["whole_graph_plain_ms"] = mean(w_ms)
+        detail["whole_graph_count_kernel_ms"] = mean(w_k)
+        for k in (2, 4, 8):
+            part = gen.parts_random(V, k)
+            row = {}
+            for mode in ("reference", "count"):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                parts = ctx.halo_extract(ug, part, k, mode=mode)
+                ctx.synchronize()
+                ext_s = time.perf_counter() - t0
+                pp_ms, _ = timed(lambda: ctx.count_each(parts))
+                assert int(ctx.count_each(parts).sum()) == whole
+                b = ctx.batch(parts)
+                assert int(b.run().sum()) == whole
+                b_ms, b_k = timed(lambda: b.run_async(), lambda: b.stats()["count_kernel_ms"])
+                outs = b.results()
+                assert int(outs.sum()) == whole, "the parts do not sum to the whole graph's count"
+                row[mode] = {"halo_extract_s": ext_s, "per_part_launches_ms": mean(pp_ms),
+                             "batched_ms": mean(b_ms), "batched_count_kernel_ms": mean(b_k),
+                             "batched_vs_per_part": mean(pp_ms) / mean(b_ms),
+                             "parts_nnz_total": int(sum(p.nnz for p in parts)),
+                             "parts_nnz_over_graph": sum(p.nnz for p in parts) / E,
+                             "parts_rows_total": int(sum(p.n_rows for p in parts)),
+                             "per_part_counts": [int(x) for x in outs]}
+                if k == 8 and mode == "count":
+                    head = (parts, b, b_ms, b_k)
+                else:
+                    b.free()
+                    del parts
+            row["batched_count_halo_vs_per_part_reference_halo"] = (row["reference"]["per_part_launches_ms"] /
+                                                                    row["count"]["batched_ms"])
+            per_k[str(k)] = row
+        detail["parts"] = per_k
+        parts, b, b_ms, b_k = head
+        ms = mean(b_ms)
+        launches = b.stats()["launches"]
+    else:
+        # sharded: the k = 8 counting parts, split over the ranks by work
+        parts_all = ctx.halo_extract(ug, gen.parts_random(V, 8), 8, mode="count")
+        work = [p.nnz for p in parts_all]
+        mine = shard.assign_parts(work, world)[rank]
+        parts = [parts_all[i] for i in mine]
+        for i, p in enumerate(parts_all):
+            if i not in mine:
+                p.free()
+        b = ctx.batch(parts) if parts else None
+        clocks.start()
+        barrier(pg)
+        torch.cuda.synchronize()
+        b_ms, b_k = timed((lambda: b.run_async()) if b else (lambda: None),
+                          (lambda: b.stats()["count_kernel_ms"]) if b else None)
+        torch.cuda.synchronize()
+        barrier(pg)
+        local_sum = int(b.results().sum()) if b else 0
+        t = torch.tensor([local_sum], dtype=torch.int64, device=dev)
+        pg.all_reduce(t)
+        assert int(t.item()) == whole, "the ranks' parts do not sum to the whole graph's count"
+        ms = mean(b_ms)
+        launches = b.stats()["launches"] if b else 0
+        detail["sharding"] = {"parts_per_rank": len(mine), "rank0_parts": mine,
+                              "assignment": "largest first by nnz (trianglecount_gb300/shard.py)"}
+    ms = max_over_ranks(ms, pg, dev)
+    value = E / (ms / 1000.0)
+
+    # ---- roofline of the batched count kernel (this rank's parts) ----
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    B_model = B_min = W_tot = 0
+    host_parts = []
+    for p in parts:
+        prp, pcol = p.download()
+        bm, bn, w = _part_bytes(prp, pcol, p.n_roots)
+        B_model, B_min, W_tot = B_model + bm, B_min + bn, W_tot + w
+        host_parts.append((prp, pcol, p.n_roots))
+    k_ms = mean(b_k) if b_k else ms
+    tr = load_traffic(f"rmat{scale}_parts_k8")
+    traffic = (tr or {}).get("traffic_bytes_per_launch")
+    sec = k_ms / 1000.0
+    roofline = {"bound": "hbm", "achieved": B_min / sec / 1e9, "peak": peak, "unit": "GB/s",
+                "frac": B_min / sec / 1e9 / peak, "traffic": traffic,
+                "peak_source": f"{peak_src} hbm_gbs (copy, burst)", "kernel": "count_kernel (batched, k = 8 parts)",
+                "kernel_ms": k_ms, "algorithmic_bytes_per_launch": B_min,
+                "algorithmic_bytes_definition": "sum over parts of 4(R+1) + 12 E_R + 4 sum_{u->v} min(d+(u), d+(v)) "
+                                                "+ 8 (R roots, E_R root edges): each root's row_ptr and list, each "
+                                                "root edge's row_ptr pair and the cheaper side's list -- the bytes "
+                                                "this design must read",
+                "dram_achieved": traffic / sec / 1e9 if traffic else None,
+                "dram_frac": traffic / sec / 1e9 / peak if traffic else None,
+                "traffic_source": (tr or {}).get("source"),
+                "survey_model_bytes": B_model, "survey_model_frac": B_model / sec / 1e9 / peak,
+                "survey_model_note": "4(R+1) + 12 E_R + 4 W+ + 8 per part (every N+(v) read): work the min-side "
+                                     "design does not do, so its fraction can exceed 1 and is not evidence",
+                "W_plus": W_tot}
+
+    # ---- end to end through the C ABI from pinned host memory (k = 8 parts) ----
+    pinned = []
+    for prp, pcol, nr in host_parts:
+        a = torch.from_numpy(prp).pin_memory()
+        c = torch.from_numpy(pcol).pin_memory()
+        pinned.append((a.numpy(), c.numpy(), nr, a, c))
+    want = [int(x) for x in b.results()] if b else []
+    e2e_ms = []
+    if pinned:
+        def e2e_call():
+            got = ctx.count_parts_csr([(q[0], q[1], q[2]) for q in pinned])
+            assert [int(x) for x in got] == want
+        e2e_ms, _ = timed(e2e_call)
+    clk = clocks.stop()
+    e2e = max_over_ranks(mean(e2e_ms), pg, dev)
+    h2d = sum(4 * len(q[0]) + 4 * len(q[1]) for q in pinned)
+
+    res = None
+    if rank == 0:
+        res = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": "int32", "data": f"synthetic (seeded R-MAT scale {scale})",
+            "config": cfg, "gpu_launches": launches * args.steps,
+            "e2e": {"value": E / (e2e / 1000.0) if e2e else None, "unit": UNIT, "ms_per_step": e2e,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 20 * len(pinned) + 48,
+                    "path": "tc_count_parts_csr_i32: upload + validate every part, one batched count, read-back"},
+            "roofline": roofline, "clocks": clk, "detail": detail,
+        }
+        if world == 1 and not args.no_ref_kernel:
+            try:
+                import oracle
+                if oracle.ref_kernel_available():
+                    oracle.ref_tc128(rp, col, runs=1)
+                    ref_ms, ok = [], True
+                    for _ in range(3):
+                        flush.zero_()
+                        torch.cuda.synchronize()
+                        pr, t_ms = oracle.ref_tc128(rp, col, runs=1)
+                        ref_ms.append(t_ms)
+                        ok = ok and int(pr.sum()) == whole
+                    rms = statistics.median(ref_ms)
+                    res["reference_gpu_kernel"] = {
+                        "value": E / (rms / 1000.0), "unit": UNIT, "ms": rms, "count_matches": ok,
+                        "source": "TC_128 Find_Triangle (ShareKernelTCV62_update_v1.cu) built from the reference "
+                                  "sources for sm_103a, on the unpartitioned graph, one 128-thread block per "
+                                  "vertex, median of 3, L2 flushed",
+                        "speedup_of_batched_parts": rms / ms,
+                        "speedup_of_whole_plain": rms / detail["whole_graph_plain_ms"]}
+            except Exception as ex:  # reported, never fatal
+                res["reference_gpu_kernel"] = {"unavailable": str(ex)[:200]}
+        if world == 1 and not args.no_cpu:
+            import oracle
+            t0 = time.perf_counter()
+            ccount = oracle.count(rp, col)
+            cdt = time.perf_counter() - t0
+            res["cpu_baseline"] = {"value": E / cdt, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+                                   "sample": f"the whole R-MAT {scale} graph, one full count (OpenMP merge "
+                                             "intersection, schedule(dynamic,64), u64 reduction); the parts sum "
+                                             "to this count",
+                                   "seconds": cdt, "count_matches": ccount == whole}
+    barrier(pg)
+    if b:
         b.free()
-    # the same graph on balanced label-propagation parts (the stand-in for the
-    # reference's METIS assignment), k = 8
-    t0 = time.perf_counter()
-    part = ctx.parts_lp(ug, 8)
-    lp_s = time.perf_counter() - t0
-    rp_u, col_u, _ = ug.download()
-    rows = np.repeat(np.arange(len(rp_u) - 1, dtype=np.int64), np.diff(rp_u))
-    cut = float((part[rows] != part[col_u]).mean())
-    del rows, rp_u, col_u
-    parts = ctx.halo_extract(ug, part, 8)
-    b = ctx.batch(parts)
-    out = b.run()
-    lp_batch_ms = _timed(stream, flush, lambda: b.run(), args.steps, args.warmup)
-    assert int(out.sum()) == whole
-    lp = {"k": 8, "partition_s": lp_s, "cut_fraction": cut, "max_part_over_mean": float(np.bincount(part).max() * 8 / V),
-          "parts_nnz": [p.nnz for p in parts], "batched_ms": lp_batch_ms, "sum_of_parts": int(out.sum())}
-    b.free()
-    del parts
-    ms = per_k["8"]["batched_ms"]
-    cfg = {"workload": "rmat23_ef16_halo_parts", "scale": 23, "edge_factor": 16, "V": V, "oriented_edges": E,
-           "triangles": whole, "parts": per_k, "whole_graph_plain_ms": whole_ms,
-           "host_generate_s": gen_s, "device_clean_s": clean_s, "device_orient_s": orient_s,
-           "partition": "seeded uniform random, k = 2, 4, 8", "lp_parts_k8": lp,
-           "l2": "flushed before every timed step (512 MiB memset on the launching stream)"}
-    res = {"metric": METRIC, "value": world * E / (ms / 1000.0), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "int32", "data": "synthetic (seeded R-MAT scale 23)", "config": cfg}
     ctx.close()
     return res
+
+
+def run_k8_batch(args, world, rank, local, pg):
+    """Profiling case: only the batched count of R-MAT's k = 8 counting-halo
+    parts, replayed warmup + steps times (the first count_kernel launch of the
+    process is the first replay's)."""
+    import torch
+
+    import trianglecount_gb300 as tc
+    from trianglecount_gb300 import generators as gen
+    torch.cuda.set_device(local)
+    ctx = tc.Context(local)
+    src, dst = gen.rmat(args.scale, 16)
+    ug = ctx.ugraph_from_edges(src, dst)
+    del src, dst
+    parts = ctx.halo_extract(ug, gen.parts_random(ug.info()[0], 8), 8, mode="count")
+    ug.free()
+    b = ctx.batch(parts)
+    ms = []
+    for _ in range(args.warmup + args.steps):
+        b.run_async()
+        b.results()
+        ms.append(b.stats()["count_kernel_ms"])
+    total = int(b.results().sum())
+    b.free()
+    ctx.close()
+    return {"workload": f"rmat{args.scale}_parts_k8_batch", "triangles": total,
+            "count_kernel_ms": ms[args.warmup:], "parts_nnz": [p.nnz for p in parts]}
 
 
 def run_batch(args, world, rank, local, pg):
@@ -765,8 +1027,8 @@ def main():
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:
-        fn = {"rmat23_parts": run_parts, "batch256": run_batch, "serve": run_serve,
-              "refstudy": run_refstudy, "io": run_io}.get(args.workload, run_ours)
+        fn = {"rmat23_parts": run_parts, "rmat23_k8_batch": run_k8_batch, "batch256": run_batch,
+              "serve": run_serve, "refstudy": run_refstudy, "io": run_io}.get(args.workload, run_ours)
         res = fn(args, world, rank, local, pg)
         if rank == 0 and res is not None:
             print(json.dumps(res), flush=True)

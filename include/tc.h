@@ -183,14 +183,21 @@ TC_API int tc_count_csr_i32(tc_ctx *ctx, const int32_t *row_ptr, const int32_t *
 /* Count without allocating: for callers that may not allocate GPU memory
  * themselves (an application that owns the device heap and forbids library
  * cudaMalloc calls, a real-time loop, a sandboxed plugin).  No counterpart in
- * the reference.  d_row_ptr / d_col are device arrays of an oriented CSR as in
- * tc_graph_upload_i32 (not validated); roots are rows [0, n_roots); the count
- * is written to the device word d_out in stream order on `stream` (a
- * cudaStream_t, NULL for the default stream).  Scratch is one fixed ~22 MB
- * device array inside libtc: at most 262,144 rows and 2,097,152 oriented edges
- * (TC_E_RANGE beyond).  Calls share that array, so calls that overlap on the
- * GPU race; the first call on a device sets up that device and should come
- * before any stream capture. */
+ * the reference.  d_row_ptr / d_col are device arrays of an oriented CSR in
+ * the form tc_graph_upload_i32 accepts: row_ptr non-decreasing from 0 to nnz,
+ * ids in [0, n_rows), rows strictly ascending.  This entry point does NOT
+ * check them (checking needs scratch and a host round trip), and a CSR that
+ * breaks them makes the kernels read outside the caller's buffers: pass only
+ * a CSR that already passed validation (for example one uploaded once with
+ * tc_graph_upload_i32 and read back, or produced by tc_orient).  Roots are
+ * rows [0, n_roots); the count is written to the device word d_out in stream
+ * order on `stream` (a cudaStream_t, NULL for the default stream); d_out
+ * receives UINT64_MAX instead if the classifier's heavy-unit list overflowed
+ * (impossible within the limits below, reported all the same).  Scratch is
+ * one fixed ~22 MB device array inside libtc: at most 262,144 rows and
+ * 2,097,152 oriented edges (TC_E_RANGE beyond).  Calls share that array, so
+ * calls that overlap on the GPU race; the first call on a device sets up that
+ * device and should come before any stream capture. */
 TC_API int tc_count_noalloc_i32(const int32_t *d_row_ptr, const int32_t *d_col, int64_t n_rows, int64_t nnz,
                                 int64_t n_roots, uint64_t *d_out, void *stream);
 
@@ -204,6 +211,20 @@ TC_API int tc_batch_run(tc_batch *b, uint64_t *outs);
 TC_API int tc_batch_run_async(tc_batch *b);             /* enqueue only */
 TC_API int tc_batch_results(tc_batch *b, uint64_t *outs); /* sync + read back */
 TC_API int tc_batch_destroy(tc_batch *b);
+/* Of the last replay: count_ms = device time of the counting kernels alone
+ * (the persistent count launch, not the classification passes), launches =
+ * kernels per replay, heavy_units as in tc_count_stats (finalize_ms = 0).
+ * Waits for that replay.  Before the first replay only launches is set. */
+TC_API int tc_batch_stats(tc_batch *b, tc_count_stats *stats);
+/* The partitioned drop-in from host memory: the parts of one graph (the
+ * u64 blocks that wo_sort_tc_256 reads, narrowed to int32 by the caller, or
+ * int32 parts from tc_halo_extract / the .tcsr cache) are uploaded and
+ * validated, counted together in one batched launch, and outs[p] (and
+ * *total, may be NULL) returned.  Replaces the per-part cudaMalloc / copy /
+ * launch / read-back loop of without_sorting_tc.cu:244-465. */
+TC_API int tc_count_parts_csr_i32(tc_ctx *ctx, int n_parts, const int32_t *const *row_ptrs,
+                                  const int32_t *const *cols, const int64_t *n_rows, const int64_t *nnz,
+                                  const int64_t *n_roots, uint64_t *outs, uint64_t *total);
 /* Per-graph launches of the same kernels with a sync after each graph: the
  * plain path the batch is compared against. */
 TC_API int tc_count_each(tc_ctx *ctx, tc_graph *const *graphs, int n_graphs, uint64_t *outs);
@@ -246,6 +267,20 @@ TC_API int tc_graph_from_edges(tc_ctx *ctx, const int64_t *src, const int64_t *d
  * the prune of Halo_creation_preprocess.py:566-589. */
 TC_API int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k, int tie,
                            tc_graph **parts_out);
+/* Halo modes of tc_halo_extract_ex.
+ * TC_HALO_REFERENCE: the parts tc_halo_extract writes (1-hop halo, zero
+ *   in-degree halo vertices peeled), the round_clean_sg file contract.
+ * TC_HALO_COUNT: only the halo vertices with an oriented in-edge from a part
+ *   vertex, and the oriented edges among the kept vertices.  A triangle
+ *   u -> v -> w rooted at a part vertex u has v and w in N+(u), so both are
+ *   kept and every part still counts exactly the triangles rooted in it (the
+ *   parts sum to the whole graph's count); the parts are smaller, so their
+ *   counts are cheaper.  Not a file format of the reference. */
+#define TC_HALO_REFERENCE 0
+#define TC_HALO_COUNT 1
+/* tc_halo_extract with a halo mode (TC_HALO_*); same part ids and layout. */
+TC_API int tc_halo_extract_ex(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k, int tie, int mode,
+                              tc_graph **parts_out);
 
 /* ---- serving: continuous batching over resident graphs ----------------------- */
 /* No counterpart in the reference (which runs one file per process).  A server

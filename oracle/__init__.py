@@ -52,11 +52,16 @@ def lib() -> C.CDLL:
         L.orc_count_brute.restype = u64
         L.orc_count_brute.argtypes = [i64, vp, vp]
         L.orc_halo_part.restype = i64
-        L.orc_halo_part.argtypes = [i64, vp, vp, vp, vp, i64, C.c_int, vp, vp, C.POINTER(i64), C.POINTER(i64)]
+        L.orc_halo_part.argtypes = [i64, vp, vp, vp, vp, i64, C.c_int, C.c_int, vp, vp, C.POINTER(i64),
+                                    C.POINTER(i64)]
         L.orc_num_threads.restype = C.c_int
         L.orc_num_threads.argtypes = []
         L.orc_read_csr_fscanf.restype = C.c_int
         L.orc_read_csr_fscanf.argtypes = [C.c_char_p, vp, C.POINTER(C.POINTER(C.c_int32)), C.POINTER(C.POINTER(C.c_int32))]
+        L.orc_gen_rmat.restype = C.c_int
+        L.orc_gen_rmat.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, u64, C.c_int, vp, vp]
+        L.orc_gen_parts_random.restype = C.c_int
+        L.orc_gen_parts_random.argtypes = [i64, C.c_int, u64, vp]
         L.orc_free.restype = None
         L.orc_free.argtypes = [vp]
         _lib = L
@@ -127,8 +132,11 @@ def count_brute(row_ptr, col) -> int:
     return int(lib().orc_count_brute(len(rp) - 1, _p(rp), _p(cl)))
 
 
-def halo_part(row_ptr, col, deg, part, p: int, tie="reference"):
-    """Halo subgraph of part p -> (row_ptr, col, t_ver), local ids."""
+def halo_part(row_ptr, col, deg, part, p: int, tie="reference", mode: str = "reference"):
+    """Halo subgraph of part p -> (row_ptr, col, t_ver), local ids.  mode
+    "reference" follows the reference's extraction; "count" keeps only the halo
+    vertices with an oriented in-edge from the part (the library's counting
+    halo)."""
     rp = np.ascontiguousarray(row_ptr, np.int64)
     cl = np.ascontiguousarray(col, np.int64)
     dg = np.ascontiguousarray(deg, np.int64)
@@ -138,7 +146,7 @@ def halo_part(row_ptr, col, deg, part, p: int, tie="reference"):
     ocl = np.empty(max(len(cl), 1), np.int64)
     nl, tv = C.c_int64(), C.c_int64()
     m = lib().orc_halo_part(V, _p(rp), _p(cl), _p(dg), _p(pt), int(p), TIE[tie] if isinstance(tie, str) else int(tie),
-                            _p(orp), _p(ocl), C.byref(nl), C.byref(tv))
+                            {"reference": 0, "count": 1}[mode], _p(orp), _p(ocl), C.byref(nl), C.byref(tv))
     return orp[:nl.value + 1].copy(), ocl[:m].copy(), tv.value
 
 
@@ -229,3 +237,29 @@ def read_csr_fscanf(path):
         L.orc_free(C.cast(rp, C.c_void_p))
         L.orc_free(C.cast(cl, C.c_void_p))
     return hdr, row_ptr, col
+
+
+# ---- seeded benchmark inputs without the library (bench.py's reference arm) ----
+RMAT_ABC = (0.57, 0.19, 0.19)
+SEED_RMAT = {16: 0x5EED0016, 21: 0x5EED0021, 23: 0x5EED0023}
+SEED_PARTS = 0x5EED9A27
+
+
+def gen_rmat(scale: int, edge_factor: int = 16, seed: int | None = None, permute: bool = True):
+    """The benchmark's R-MAT edge list (same bits as the library's generator)."""
+    n = edge_factor << scale
+    src = np.empty(n, np.int64)
+    dst = np.empty(n, np.int64)
+    seed = SEED_RMAT.get(scale, 0x5EED0000 + scale) if seed is None else seed
+    a, b, c = RMAT_ABC
+    if lib().orc_gen_rmat(scale, edge_factor, a, b, c, seed, 1 if permute else 0, _p(src), _p(dst)) != 0:
+        raise ValueError("bad R-MAT parameters")
+    return src, dst
+
+
+def gen_parts_random(n: int, k: int, seed: int | None = None):
+    """Seeded uniform parts (same bits as the library's generator)."""
+    part = np.empty(n, np.int32)
+    if lib().orc_gen_parts_random(n, k, (SEED_PARTS + k) if seed is None else seed, _p(part)) != 0:
+        raise ValueError("bad partition arguments")
+    return part

@@ -1,6 +1,7 @@
 #!/usr/bin/env bash
 # Builds checkers from the reference's own sources, in place, into oracle/_ref/
-# (git-ignored).  Test infrastructure only; needs the reference tree at $REF.
+# (git-ignored).  Test infrastructure only; needs the reference tree at $REF
+# (default: ../reference relative to the repository root).
 #
 #   undir2dir             preprocess_CPU/Undir2Dir.c, the reference's CPU degree
 #                         orientation (pins oracle.c:orc_orient)
@@ -18,8 +19,10 @@
 # to show it builds; its kernel calls __syncthreads() inside `if (tid == 0)`
 # (without_sorting_tc.cu:209-217), so it is never launched.
 set -euo pipefail
-REF=${REF:-/root/reference}
-OUT="$(cd "$(dirname "$0")" && pwd)/_ref"
+HERE="$(cd "$(dirname "$0")" && pwd)"
+# the reference tree: $REF, else a checkout named "reference" beside the repository
+REF=${REF:-"$(dirname "$(dirname "$HERE")")/reference"}
+OUT="$HERE/_ref"
 NVCC=${NVCC:-/usr/local/cuda/bin/nvcc}
 [ -d "$REF" ] || { echo "reference tree not found at $REF; skipping"; exit 0; }
 mkdir -p "$OUT"

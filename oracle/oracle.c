@@ -29,11 +29,22 @@
  *                    with the prune loop of
  *                    preprocess_GPU/generate_clean_undir_dataset/Halo_creation_preprocess.py:566-589
  *
+ *   orc_gen_rmat / orc_gen_parts_random  the benchmark's seeded inputs,
+ *                    generated without the library so that the reference arm
+ *                    of bench.py loads no product code: R-MAT quadrant draws
+ *                    of 16 bits from the splitmix64 output function applied
+ *                    to (seed, stream, index), a Fisher-Yates vertex
+ *                    permutation, and uniform parts (they replace the
+ *                    unseeded np.random.randint of
+ *                    Halo_creation_preprocess.py:288); the tests check them
+ *                    bit for bit against the library's generators
+ *
  * Tie-break: the reference keeps u->w iff deg(u) < deg(w), or deg(u) == deg(w)
  * and w < u (without_part_preprocess.py:37-50).  ORC_TIE_ID_ASC selects the
  * other strict order, (deg u, u) < (deg w, w).  Both orient every undirected
  * edge exactly once, so the count is the same; the files differ.
  */
+#include <math.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -340,11 +351,16 @@ uint64_t orc_count_brute(int64_t V, const int64_t *row_ptr, const int64_t *col)
  *     until none is left (the intended loop, Halo_creation_preprocess.py:566-589;
  *     round_clean_subgraph.cu:671-838 implements round 1 correctly only).
  *
+ * mode 1 (the library's counting halo, which has no reference counterpart):
+ * step 2 keeps only the neighbours d of P outside P with s -> d kept by the
+ * orientation rule for some s in P; steps 3-5 are unchanged (step 5 then
+ * removes nothing: every halo vertex keeps its in-edge from P).
+ *
  * Buffers: out_row_ptr capacity V+1, out_col capacity row_ptr[V].
  * Outputs *n_local, *t_ver; returns the local nnz.
  */
 int64_t orc_halo_part(int64_t V, const int64_t *row_ptr, const int64_t *col, const int64_t *deg,
-                      const int64_t *part, int64_t p, int tie, int64_t *out_row_ptr, int64_t *out_col,
+                      const int64_t *part, int64_t p, int tie, int mode, int64_t *out_row_ptr, int64_t *out_col,
                       int64_t *n_local_out, int64_t *t_ver_out)
 {
     int64_t *lid = (int64_t *)malloc(sizeof(int64_t) * (size_t)(V ? V : 1));
@@ -357,7 +373,8 @@ int64_t orc_halo_part(int64_t V, const int64_t *row_ptr, const int64_t *col, con
     for (int64_t v = 0; v < V; v++) {
         if (part[v] != p) continue;
         for (int64_t j = row_ptr[v]; j < row_ptr[v + 1]; j++)
-            if (part[col[j]] != p) inH[col[j]] = 1;
+            if (part[col[j]] != p && (mode == 0 || keep_edge(deg[v], deg[col[j]], v, col[j], tie)))
+                inH[col[j]] = 1;
     }
     int64_t n_comb = t_ver;
     for (int64_t v = 0; v < V; v++)
@@ -462,3 +479,77 @@ fail:
 }
 
 void orc_free(void *p) { free(p); }
+
+/* ---- seeded inputs (independent of the library) ------------------------- */
+/* splitmix64's output function (Steele, Lea, Flood, OOPSLA 2014) on a counter */
+static uint64_t orc_mix(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+/* draw i of stream `stream` under `seed` */
+static uint64_t orc_draw(uint64_t seed, uint64_t stream, uint64_t i)
+{
+    return orc_mix(orc_mix(seed ^ (stream * 0xD1B54A32D192ED03ull)) + i);
+}
+
+/* r mapped onto [0, range) by the high half of the 128-bit product (Lemire) */
+static uint64_t orc_below(uint64_t r, uint64_t range)
+{
+    return (uint64_t)(((unsigned __int128)r * range) >> 64);
+}
+
+/* R-MAT: edge_factor << scale edges; at each of `scale` levels a 16-bit draw
+ * picks quadrant (0,0) below a, (0,1) below a+b, (1,0) below a+b+c, else
+ * (1,1) (probabilities as 16-bit fixed point, rounded); four levels share one
+ * 64-bit draw (stream 1, index 8 i + level / 4).  permute != 0 relabels by a
+ * Fisher-Yates shuffle (stream 2, index = the position swapped down). */
+int orc_gen_rmat(int scale, int edge_factor, double a, double b, double c, uint64_t seed, int permute,
+                 int64_t *src, int64_t *dst)
+{
+    if (scale < 1 || scale > 31 || edge_factor < 1) return -1;
+    const int64_t n = (int64_t)edge_factor << scale, nv = (int64_t)1 << scale;
+    const uint32_t qa = (uint32_t)llround(a * 65536.0), qab = (uint32_t)llround((a + b) * 65536.0),
+                   qabc = (uint32_t)llround((a + b + c) * 65536.0);
+    int64_t *perm = NULL;
+    if (permute) {
+        perm = (int64_t *)malloc(sizeof(int64_t) * (size_t)nv);
+        if (!perm) return -1;
+        for (int64_t i = 0; i < nv; i++) perm[i] = i;
+        for (int64_t i = nv - 1; i > 0; i--) {
+            const int64_t j = (int64_t)orc_below(orc_draw(seed, 2, (uint64_t)i), (uint64_t)i + 1);
+            const int64_t t = perm[i];
+            perm[i] = perm[j];
+            perm[j] = t;
+        }
+    }
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < n; e++) {
+        int64_t u = 0, v = 0;
+        uint64_t bits = 0;
+        for (int l = 0; l < scale; l++) {
+            if (l % 4 == 0) bits = orc_draw(seed, 1, (uint64_t)e * 8 + (uint64_t)(l / 4));
+            const uint32_t r = (uint32_t)(bits & 0xFFFFu);
+            bits >>= 16;
+            const int right = r >= qabc || (r >= qa && r < qab);
+            const int down = r >= qab;
+            u = 2 * u + down;
+            v = 2 * v + right;
+        }
+        src[e] = permute ? perm[u] : u;
+        dst[e] = permute ? perm[v] : v;
+    }
+    free(perm);
+    return 0;
+}
+
+/* part[v] uniform in [0, k) (stream 5, index v) */
+int orc_gen_parts_random(int64_t n, int k, uint64_t seed, int32_t *part)
+{
+    if (n < 0 || k < 1) return -1;
+    for (int64_t v = 0; v < n; v++) part[v] = (int32_t)orc_below(orc_draw(seed, 5, (uint64_t)v), (uint64_t)k);
+    return 0;
+}

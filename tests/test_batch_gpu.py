@@ -55,3 +55,33 @@ def test_batch_mixes_degenerate_and_bounded_degree_graphs(ctx):
     for _ in range(2):
         assert list(b.run()) == want
     b.free()
+
+
+def test_batch_stats_and_parts_from_host(ctx):
+    """tc_batch_stats times the replay's counting kernels; tc_count_parts_csr_i32
+    counts halo parts from host arrays in one launch, exactly as the oracle."""
+    src, dst = gen.rmat(13)
+    rp, col = oracle.clean(src, dst)
+    whole = oracle.count(*oracle.orient(rp, col))
+    part = gen.parts_random(len(rp) - 1, 4)
+    host = [oracle.halo_part(rp, col, np.diff(rp), part, p, mode="count") for p in range(4)]
+    want = [oracle.count(lrp, lcol, n_roots=t) for lrp, lcol, t in host]
+    got = ctx.count_parts_csr([(lrp.astype(np.int32), lcol.astype(np.int32), t) for lrp, lcol, t in host])
+    assert list(got) == want and sum(want) == whole
+    graphs = [ctx.upload(lrp, lcol, n_roots=t) for lrp, lcol, t in host]
+    b = ctx.batch(graphs)
+    st0 = b.stats()
+    assert st0["launches"] > 0 and st0["count_kernel_ms"] == 0.0
+    assert list(b.run()) == want
+    st = b.stats()
+    assert st["count_kernel_ms"] > 0.0 and st["launches"] == st0["launches"]
+    b.free()
+
+
+def test_parts_from_host_rejects_a_bad_part(ctx):
+    import trianglecount_gb300 as tc
+    rp = np.array([0, 2, 3, 3], np.int32)
+    bad = np.array([2, 1, 2], np.int32)  # row 0 not ascending
+    with pytest.raises(tc.TCError) as e:
+        ctx.count_parts_csr([(rp, np.array([1, 2, 2], np.int32), 3), (rp, bad, 3)])
+    assert e.value.code == "TC_E_FORMAT"

@@ -9,9 +9,10 @@ from trianglecount_gb300 import generators as gen
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("mode", ["reference", "count"])
 @pytest.mark.parametrize("k", [1, 2, 4, 8])
 @pytest.mark.parametrize("maker", ["rmat13", "road", "chung_lu"])
-def test_halo_parts_match_oracle(ctx, k, maker):
+def test_halo_parts_match_oracle(ctx, k, maker, mode):
     if maker == "rmat13":
         src, dst = gen.rmat(13)
     elif maker == "road":
@@ -23,10 +24,10 @@ def test_halo_parts_match_oracle(ctx, k, maker):
     whole = oracle.count(*oracle.orient(rp, col))
     part = gen.parts_random(len(rp) - 1, k)
     ug = ctx.upload_ugraph(rp, col, deg)
-    parts = ctx.halo_extract(ug, part, k)
+    parts = ctx.halo_extract(ug, part, k, mode=mode)
     total = 0
     for p, g in enumerate(parts):
-        lrp, lcol, t_ver = oracle.halo_part(rp, col, deg, part, p)
+        lrp, lcol, t_ver = oracle.halo_part(rp, col, deg, part, p, mode=mode)
         drp, dcol = g.download()
         assert g.n_roots == t_ver
         assert np.array_equal(drp, lrp) and np.array_equal(dcol, lcol), (maker, k, p)
@@ -72,8 +73,9 @@ def test_halo_tile_boundaries(ctx, n, k):
     assert total == oracle.count(*oracle.orient(rp, col)) == n
 
 
+@pytest.mark.parametrize("mode", ["reference", "count"])
 @pytest.mark.parametrize("k, n_labels", [(40, 40), (3, 5), (3, 36)])
-def test_halo_many_parts_and_unassigned_vertices(ctx, k, n_labels):
+def test_halo_many_parts_and_unassigned_vertices(ctx, k, n_labels, mode):
     """k > 32 takes the per-part halo pass instead of the all-parts masks;
     labels >= k (also >= 32) put vertices in no extracted part, though they
     can still be in a part's halo."""
@@ -82,10 +84,28 @@ def test_halo_many_parts_and_unassigned_vertices(ctx, k, n_labels):
     deg = np.diff(rp)
     part = np.random.default_rng(k * 100 + n_labels).integers(0, n_labels, len(rp) - 1).astype(np.int32)
     ug = ctx.upload_ugraph(rp, col, deg)
-    parts = ctx.halo_extract(ug, part, k)
+    parts = ctx.halo_extract(ug, part, k, mode=mode)
     assert len(parts) == k
     for p, g in enumerate(parts):
-        lrp, lcol, t_ver = oracle.halo_part(rp, col, deg, part, p)
+        lrp, lcol, t_ver = oracle.halo_part(rp, col, deg, part, p, mode=mode)
         drp, dcol = g.download()
         assert g.n_roots == t_ver
         assert np.array_equal(drp, lrp) and np.array_equal(dcol, lcol), (k, n_labels, p)
+
+
+@pytest.mark.parametrize("tie", ["reference", "id_asc"])
+def test_counting_halo_tie_breaks(ctx, tie):
+    """Both tie-breaks: the counting halo follows the orientation's own rule."""
+    src, dst = gen.rmat(12)
+    rp, col = oracle.clean(src, dst)
+    deg = np.diff(rp)
+    part = gen.parts_random(len(rp) - 1, 4)
+    ug = ctx.upload_ugraph(rp, col, deg)
+    whole = oracle.count(*oracle.orient(rp, col, tie))
+    total = 0
+    for p, g in enumerate(ctx.halo_extract(ug, part, 4, tie=tie, mode="count")):
+        lrp, lcol, t_ver = oracle.halo_part(rp, col, deg, part, p, tie=tie, mode="count")
+        drp, dcol = g.download()
+        assert np.array_equal(drp, lrp) and np.array_equal(dcol, lcol), (tie, p)
+        total += ctx.count(g)
+    assert total == whole

@@ -122,6 +122,33 @@ def test_halo_parts_sum_to_whole(k):
     assert total == whole
 
 
+@pytest.mark.parametrize("k", [2, 4, 8])
+def test_counting_halo_parts_sum_to_whole_and_shrink(k):
+    """The counting halo keeps the halo vertices with an oriented in-edge from
+    the part: each part's count is unchanged, and the parts are subgraphs of
+    the reference parts (fewer or equal rows and entries)."""
+    src, dst = gen.chung_lu(20000, 10.0, seed=3)
+    rp, col = oracle.clean(src, dst)
+    deg = np.diff(rp)
+    orp, ocl = oracle.orient(rp, col)
+    whole = oracle.count(orp, ocl)
+    part = gen.parts_random(len(rp) - 1, k)
+    rows = np.repeat(np.arange(len(orp) - 1), np.diff(orp))
+    total = 0
+    for p in range(k):
+        lrp, lcol, t_ver = oracle.halo_part(rp, col, deg, part, p, mode="count")
+        rrp, rcol, rt = oracle.halo_part(rp, col, deg, part, p)
+        assert t_ver == rt and len(lrp) <= len(rrp) and len(lcol) <= len(rcol)
+        # the halo is exactly the oriented out-neighbours of the part outside it
+        inP = part == p
+        want_halo = np.unique(ocl[inP[rows] & ~inP[ocl]])
+        assert len(lrp) - 1 == t_ver + len(want_halo)
+        c = oracle.count(lrp, lcol, n_roots=t_ver)
+        assert c == oracle.count(rrp, rcol, n_roots=rt)
+        total += c
+    assert total == whole
+
+
 def test_planted_orientation_mistake_is_caught():
     """A non-strict orientation (keep u->w when degrees tie both ways) double
     counts; the known-answer check must notice."""
@@ -161,3 +188,14 @@ def test_fscanf_reader_matches_parallel_parser(tmp_path):
     p.write_text(p.read_text()[: len(p.read_text()) // 2])  # ends early
     with pytest.raises(OSError):
         oracle.read_csr_fscanf(p)
+
+
+@pytest.mark.parametrize("scale, permute", [(10, True), (13, True), (12, False)])
+def test_oracle_generators_match_the_library(scale, permute):
+    """The reference arm of bench.py builds its input with the oracle's
+    generators (no library loaded); they must give the library's bits."""
+    s1, d1 = oracle.gen_rmat(scale, permute=permute)
+    s2, d2 = gen.rmat(scale, permute=permute)
+    assert np.array_equal(s1, s2) and np.array_equal(d1, d2)
+    for k in (2, 8):
+        assert np.array_equal(oracle.gen_parts_random(5000, k), gen.parts_random(5000, k))

@@ -17,6 +17,7 @@ STATUS = {
     -6: "TC_E_IO", -7: "TC_E_NOT_READY", -8: "TC_E_TIMEOUT", -9: "TC_E_NO_DEVICE", -10: "TC_E_STATE",
 }
 TIE = {"reference": 0, "id_asc": 1}
+HALO = {"reference": 0, "count": 1}  # tc_halo_extract_ex modes (TC_HALO_*)
 
 
 class TCError(RuntimeError):
@@ -88,6 +89,8 @@ _SIGS = {
     "tc_batch_run_async": (C.c_int, [vp]),
     "tc_batch_results": (C.c_int, [vp, vp]),
     "tc_batch_destroy": (C.c_int, [vp]),
+    "tc_batch_stats": (C.c_int, [vp, P(CountStats)]),
+    "tc_count_parts_csr_i32": (C.c_int, [vp, C.c_int, P(vp), P(vp), P(i64), P(i64), P(i64), vp, P(u64)]),
     "tc_count_each": (C.c_int, [vp, P(vp), C.c_int, vp]),
     "tc_ugraph_from_edges": (C.c_int, [vp, vp, vp, i64, i64, P(vp)]),
     "tc_ugraph_upload_i64": (C.c_int, [vp, vp, vp, vp, i64, i64, P(vp)]),
@@ -97,6 +100,7 @@ _SIGS = {
     "tc_orient": (C.c_int, [vp, vp, C.c_int, P(vp)]),
     "tc_graph_from_edges": (C.c_int, [vp, vp, vp, i64, i64, C.c_int, P(vp)]),
     "tc_halo_extract": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, P(vp)]),
+    "tc_halo_extract_ex": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.c_int, P(vp)]),
     "tc_server_create": (C.c_int, [vp, P(ServerConfig), P(vp)]),
     "tc_server_submit": (C.c_int, [vp, u64, vp, vp, i64, i64, P(u64)]),
     "tc_server_poll": (C.c_int, [vp, u64, P(u64), P(C.c_double)]),

@@ -143,6 +143,13 @@ class Batch:
         N.call("tc_batch_results", self._h, _ptr(self._out))
         return self._out.copy()
 
+    def stats(self) -> dict:
+        """Of the last replay: counting-kernel device time (ms), kernels per
+        replay, heavy block units."""
+        st = N.CountStats()
+        N.call("tc_batch_stats", self._h, C.byref(st))
+        return {"count_kernel_ms": st.count_ms, "launches": st.launches, "heavy_units": st.heavy_units}
+
     def free(self) -> None:
         if getattr(self, "_h", None) is not None:
             N.lib().tc_batch_destroy(self._h)
@@ -324,6 +331,22 @@ class Context:
         N.call("tc_count_csr_i32", self._h, _ptr(rp), _ptr(cl), len(rp) - 1, len(cl), C.byref(out))
         return out.value
 
+    def count_parts_csr(self, parts: Sequence[tuple]) -> np.ndarray:
+        """The partitioned path from host arrays: parts = [(row_ptr, col,
+        n_roots), ...] (int32); upload, validate, one batched count."""
+        rps = [np.ascontiguousarray(p[0], np.int32) for p in parts]
+        cls = [np.ascontiguousarray(p[1], np.int32) for p in parts]
+        n = len(parts)
+        arr_rp = (C.c_void_p * n)(*[a.ctypes.data for a in rps])
+        arr_cl = (C.c_void_p * n)(*[a.ctypes.data for a in cls])
+        nr = (C.c_int64 * n)(*[len(a) - 1 for a in rps])
+        nz = (C.c_int64 * n)(*[len(a) for a in cls])
+        ro = (C.c_int64 * n)(*[int(p[2]) for p in parts])
+        out = np.empty(n, np.uint64)
+        tot = C.c_uint64()
+        N.call("tc_count_parts_csr_i32", self._h, n, arr_rp, arr_cl, nr, nz, ro, _ptr(out), C.byref(tot))
+        return out
+
     def count_each(self, graphs: Sequence[Graph]) -> np.ndarray:
         arr = (C.c_void_p * len(graphs))(*[g.handle for g in graphs])
         out = np.empty(len(graphs), np.uint64)
@@ -371,8 +394,14 @@ class Context:
         N.call("tc_gen_parts_lp", self._h, ug.handle, int(k), int(seed), int(iterations), _ptr(out))
         return out
 
-    def halo_extract(self, ug: UGraph, part: np.ndarray, k: int, tie="reference") -> list[Graph]:
+    def halo_extract(self, ug: UGraph, part: np.ndarray, k: int, tie="reference", mode="reference") -> list[Graph]:
+        """Per-part halo subgraphs.  mode "reference": the round_clean_sg parts
+        (1-hop halo, zero-in-degree halo peeled); "count": only halo vertices
+        with an oriented in-edge from the part (smaller, same per-part counts)."""
         p = np.ascontiguousarray(part, np.int32)
         outs = (C.c_void_p * k)()
-        N.call("tc_halo_extract", self._h, ug.handle, _ptr(p), int(k), _tie(tie), outs)
+        if mode == "reference":
+            N.call("tc_halo_extract", self._h, ug.handle, _ptr(p), int(k), _tie(tie), outs)
+        else:
+            N.call("tc_halo_extract_ex", self._h, ug.handle, _ptr(p), int(k), _tie(tie), N.HALO[mode], outs)
         return [Graph(self, C.c_void_p(outs[i])) for i in range(k)]

@@ -861,6 +861,9 @@ struct tc_batch {
     int64_t total_vertices = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    cudaEvent_t kev[2] = {nullptr, nullptr};  // around the counting kernels, recorded by every replay
+    int launches = 0;                         // kernels per replay
+    bool ran = false;
 };
 
 extern "C" {
@@ -871,6 +874,8 @@ int tc_batch_destroy(tc_batch *b) {
     if (s) cudaStreamSynchronize(s);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
+    for (auto &e : b->kev)
+        if (e) cudaEventDestroy(e);
     dfree(b->d_desc, s);
     scratch_free(&b->sc, s);
     dfree(b->d_work, s);
@@ -924,12 +929,14 @@ int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out)
                                        s) != cudaSuccess)
         st = set_error(TC_E_CUDA, "descriptor upload failed");
     if (st == TC_OK && cudaStreamSynchronize(s) != cudaSuccess) st = set_error(TC_E_CUDA, "batch setup sync failed");
+    for (int i = 0; i < 2 && st == TC_OK; ++i)
+        if (cudaEventCreate(&b->kev[i]) != cudaSuccess) st = set_error(TC_E_CUDA, "event creation failed");
     // capture [memset -> classify -> count] once; tc_batch_run replays it
     if (st == TC_OK && cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         st = set_error(TC_E_CUDA, "stream capture could not start");
     if (st == TC_OK) {
         int ls = launch_count(b->d_desc, n, chunks, vtot, max_rows, b->sc, b->d_work,
-                              (unsigned long long *)(b->d_work + 1), false, ctx->tuned, s, nullptr);
+                              (unsigned long long *)(b->d_work + 1), false, ctx->tuned, s, &b->launches, b->kev);
         cudaError_t e = cudaStreamEndCapture(s, &b->graph);
         if (ls != TC_OK) st = ls;
         else if (e != cudaSuccess) st = cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
@@ -949,7 +956,40 @@ int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out)
 int tc_batch_run_async(tc_batch *b) {
     if (!b) return set_error(TC_E_INVALID, "null batch");
     TC_CUDA(cudaGraphLaunch(b->exec, b->ctx->stream));
+    b->ran = b->total_chunks > 0;
     return TC_OK;
+}
+
+int tc_batch_stats(tc_batch *b, tc_count_stats *stats) {
+    if (!b || !stats) return set_error(TC_E_INVALID, "null argument");
+    memset(stats, 0, sizeof *stats);
+    stats->launches = b->launches;
+    if (!b->ran) return TC_OK;
+    TC_CUDA(cudaEventSynchronize(b->kev[1]));
+    TC_CUDA(cudaEventElapsedTime(&stats->count_ms, b->kev[0], b->kev[1]));
+    CountWork w;
+    TC_CUDA(cudaMemcpy(&w, b->d_work, sizeof w, cudaMemcpyDeviceToHost));
+    stats->heavy_units = (int32_t)(w.heavy_packed & 0xffffffffull);
+    return TC_OK;
+}
+
+int tc_count_parts_csr_i32(tc_ctx *ctx, int n_parts, const int32_t *const *row_ptrs, const int32_t *const *cols,
+                           const int64_t *n_rows, const int64_t *nnz, const int64_t *n_roots, uint64_t *outs,
+                           uint64_t *total) {
+    if (!ctx || n_parts <= 0 || !row_ptrs || !cols || !n_rows || !nnz || !n_roots || !outs)
+        return set_error(TC_E_INVALID, "null argument or no parts");
+    std::vector<tc_graph *> gs((size_t)n_parts, nullptr);
+    int st = TC_OK;
+    for (int p = 0; p < n_parts && st == TC_OK; ++p)
+        st = tc_graph_upload_i32(ctx, row_ptrs[p], cols[p], n_rows[p], nnz[p], n_roots[p], &gs[(size_t)p]);
+    if (st == TC_OK) st = count_graphs_direct(ctx, gs.data(), n_parts, outs, 0, nullptr);
+    for (tc_graph *g : gs) tc_graph_destroy(g);
+    if (st == TC_OK && total) {
+        uint64_t t = 0;
+        for (int p = 0; p < n_parts; ++p) t += outs[p];
+        *total = t;
+    }
+    return st;
 }
 
 int tc_batch_results(tc_batch *b, uint64_t *outs) {

@@ -17,6 +17,14 @@
 // call on a device looks up the array's device address and the kernel
 // configuration for that device (cudaGetSymbolAddress, occupancy query); make
 // that first call before any stream capture.
+//
+// Every device-side step of a call is a kernel launch or a device-to-device
+// memset in stream order: the graph descriptor travels as a kernel parameter
+// (no copy from host memory), and the result is written by a one-thread
+// kernel, which stores all ones (UINT64_MAX) in place of the count if the
+// classifier's heavy-unit list overflowed (it cannot for a CSR within the
+// limits: each row gives at most one heavy entry and the list has a slot per
+// row).
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -53,6 +61,17 @@ struct DeviceSetup {
     unsigned char *scratch = nullptr;  // device address of g_noalloc_scratch
     Tuned tuned{};
 };
+
+// The descriptor of one call, written in stream order from a kernel
+// parameter (a host-to-device copy from the caller's stack would stage
+// through pageable memory).
+__global__ void noalloc_set_desc_kernel(GraphDesc *dst, GraphDesc d) { *dst = d; }
+
+// d_out = the count, or all ones when the heavy-unit list overflowed.
+__global__ void noalloc_finish_kernel(const CountWork *work, const unsigned long long *result,
+                                      unsigned long long *d_out) {
+    *d_out = work->error ? ~0ull : *result;
+}
 
 std::mutex g_setup_mu;
 DeviceSetup g_setup[64];
@@ -126,9 +145,11 @@ extern "C" int tc_count_noalloc_i32(const int32_t *d_row_ptr, const int32_t *d_c
     d.col = d_col;
     d.n_rows = n_rows;
     d.n_roots = n_roots;
-    TC_CUDA(cudaMemcpyAsync(desc, &d, sizeof d, cudaMemcpyHostToDevice, s));
+    noalloc_set_desc_kernel<<<1, 1, 0, s>>>(desc, d);
+    TC_CUDA(cudaGetLastError());
     TC_TRY(launch_count_noalloc(desc, (n_rows + 31) / 32, n_rows + 1, sc, (int32_t *)(base + kOffScan), kScanTmp,
                                 work, result, ds->tuned, s));
-    TC_CUDA(cudaMemcpyAsync(d_out, result, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+    noalloc_finish_kernel<<<1, 1, 0, s>>>(work, result, (unsigned long long *)d_out);
+    TC_CUDA(cudaGetLastError());
     return TC_OK;
 }

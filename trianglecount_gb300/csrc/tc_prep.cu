@@ -320,16 +320,20 @@ __global__ void __launch_bounds__(kOT) orient_tile_write_kernel(const int32_t *_
 // neighbour of v in part q, so v is in part p's halo when bit p is set and
 // part[v] != p (the undirected CSR is symmetric: v has a neighbour in p iff
 // some vertex of p has v as a neighbour).  One atomicOr per row run of a
-// thread's 16 entries.
+// thread's 16 entries.  With `in_only` (the counting halo) a neighbour w in
+// part q sets bit q only when w -> v is the oriented direction, so the halo
+// of part p is the set of vertices with an oriented in-edge from p.
 __global__ void __launch_bounds__(kOT) halo_mask_kernel(const int32_t *__restrict__ rowid,
                                                          const int32_t *__restrict__ col,
-                                                         const int32_t *__restrict__ part, int64_t nnz,
-                                                         unsigned *__restrict__ mask) {
+                                                         const int32_t *__restrict__ part,
+                                                         const int32_t *__restrict__ deg, int64_t nnz, int in_only,
+                                                         int tie, unsigned *__restrict__ mask) {
     int u[kOI], w[kOI];
     const int64_t j0 = (int64_t)blockIdx.x * kOTile + (int64_t)threadIdx.x * kOI;
     if (j0 >= nnz) return;
     load16(rowid, col, j0, nnz, u, w);
     int cur = u[0];
+    int dcur = in_only ? __ldg(deg + cur) : 0;
     unsigned m = 0;
 #pragma unroll
     for (int i = 0; i < kOI; ++i) {
@@ -337,10 +341,11 @@ __global__ void __launch_bounds__(kOT) halo_mask_kernel(const int32_t *__restric
         if (u[i] != cur) {
             if (m) atomicOr(mask + cur, m);
             cur = u[i];
+            if (in_only) dcur = __ldg(deg + cur);
             m = 0;
         }
         const unsigned q = (unsigned)__ldg(part + w[i]);
-        if (q < 32u) m |= 1u << q;
+        if (q < 32u && (!in_only || keep_edge(__ldg(deg + w[i]), dcur, w[i], cur, tie))) m |= 1u << q;
     }
     if (m) atomicOr(mask + cur, m);
 }
@@ -359,11 +364,11 @@ __global__ void part_flags_kernel(const int32_t *part, int64_t n, int p, uint8_t
     GRID_STRIDE(v, n) inP[v] = (uint8_t)(part[v] == p);
 }
 
-__global__ void halo_flags_kernel(const int32_t *rowid, const int32_t *col, int64_t nnz, const int32_t *part, int p,
-                                  uint8_t *inH) {
+__global__ void halo_flags_kernel(const int32_t *rowid, const int32_t *col, int64_t nnz, const int32_t *part,
+                                  const int32_t *deg, int p, int in_only, int tie, uint8_t *inH) {
     GRID_STRIDE(j, nnz) {
-        const int d = col[j];
-        if (part[rowid[j]] == p && part[d] != p) inH[d] = 1;
+        const int s = rowid[j], d = col[j];
+        if (part[s] == p && part[d] != p && (!in_only || keep_edge(deg[s], deg[d], s, d, tie))) inH[d] = 1;
     }
 }
 
@@ -895,8 +900,15 @@ int tc_graph_from_edges(tc_ctx *ctx, const int64_t *src, const int64_t *dst, int
 }
 
 int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k, int tie, tc_graph **parts_out) {
+    return tc_halo_extract_ex(ctx, ug, part, k, tie, TC_HALO_REFERENCE, parts_out);
+}
+
+int tc_halo_extract_ex(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k, int tie, int mode,
+                       tc_graph **parts_out) {
     if (!ug || !part || k < 1 || !parts_out || (tie != TC_TIE_REFERENCE && tie != TC_TIE_ID_ASC))
         return set_error(TC_E_INVALID, "bad halo arguments");
+    if (mode != TC_HALO_REFERENCE && mode != TC_HALO_COUNT) return set_error(TC_E_INVALID, "bad halo mode %d", mode);
+    const int in_only = mode == TC_HALO_COUNT;
     if (!ctx) ctx = ug->ctx;
     for (int p = 0; p < k; ++p) parts_out[p] = nullptr;
     cudaStream_t s = ctx->stream;
@@ -929,7 +941,9 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
     if (masks) {
         TC_TRY(mask.alloc((size_t)std::max<int64_t>(V, 1), s));
         TC_CUDA(cudaMemsetAsync(mask.p, 0, sizeof(uint32_t) * (size_t)std::max<int64_t>(V, 1), s));
-        if (tiles) halo_mask_kernel<<<(unsigned)tiles, kOT, 0, s>>>(ug->rowid, ug->col, dpart.p, nnz, mask.p);
+        if (tiles)
+            halo_mask_kernel<<<(unsigned)tiles, kOT, 0, s>>>(ug->rowid, ug->col, dpart.p, ug->deg, nnz, in_only, tie,
+                                                              mask.p);
         TC_CUDA(cudaGetLastError());
     }
     // one part; any failure returns its status (the caller frees all parts)
@@ -939,7 +953,8 @@ int tc_halo_extract(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *part, int k
         } else {
             if (V) part_flags_kernel<<<gV, 256, 0, s>>>(dpart.p, V, p, inP.p);
             TC_CUDA(cudaMemsetAsync(inH.p, 0, (size_t)V, s));
-            if (nnz) halo_flags_kernel<<<gE, 256, 0, s>>>(ug->rowid, ug->col, nnz, dpart.p, p, inH.p);
+            if (nnz)
+                halo_flags_kernel<<<gE, 256, 0, s>>>(ug->rowid, ug->col, nnz, dpart.p, ug->deg, p, in_only, tie, inH.p);
         }
         TC_CUDA(cudaGetLastError());
         TC_TRY(scan_flags_u8(inP.p, lidP.p, V, s));
