@@ -313,8 +313,7 @@ def run_ours(args, world, rank, local, pg):
     for _ in range(args.warmup):
         one_step(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
     torch.cuda.synchronize()
-    count = int(d_out.item())
-    _, st0 = ctx.count(g, stats=True)
+    count, st0 = ctx.count(g, stats=True)
     launches_per_count = int(st0["launches"])
 
     clocks = ClockSampler(local)
@@ -455,7 +454,9 @@ def run_ours(args, world, rank, local, pg):
     return res
 
 
-def _timed(stream, flush, fn, steps, warmup):
+def _timed(stream, flush, fn, steps, warmup, after=None):
+    """Mean device time (CUDA events on `stream`) of fn over `steps` runs after
+    `warmup`, L2 flushed before each; after() runs once each step has ended."""
     import torch
     ms = []
     for i in range(warmup + steps):
@@ -467,6 +468,8 @@ def _timed(stream, flush, fn, steps, warmup):
         with torch.cuda.stream(stream):
             e1.record(stream)
         e1.synchronize()
+        if after is not None:
+            after()
         if i >= warmup:
             ms.append(e0.elapsed_time(e1))
     return sum(ms) / len(ms)
@@ -821,6 +824,13 @@ def run_k8_batch(args, world, rank, local, pg):
             "count_kernel_ms": ms[args.warmup:], "parts_nnz": [p.nnz for p in parts]}
 
 
+def _peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
 def run_batch(args, world, rank, local, pg):
     """Uneven batch: 256 seeded ER / Chung-Lu / R-MAT graphs, one launch per
     graph (host sync after each) versus one persistent launch for all."""
@@ -849,23 +859,63 @@ def run_batch(args, world, rank, local, pg):
     b = ctx.batch(graphs)
     outs = b.run()
     assert list(outs) == list(each)
+    host = [g.download() for g in graphs]
     # oracle spot check on the smallest graphs
     small = sorted(range(len(specs)), key=lambda i: graphs[i].nnz)[:8]
     for i in small:
-        rp, col = graphs[i].download()
-        assert oracle.count(rp, col) == int(outs[i])
+        assert oracle.count(*host[i]) == int(outs[i])
+    clocks = ClockSampler(local)
+    clocks.start()
     plain_ms = _timed(stream, flush, lambda: ctx.count_each(graphs), args.steps, args.warmup)
-    batch_ms = _timed(stream, flush, lambda: b.run(), args.steps, args.warmup)
+    kms = []
+    batch_ms = _timed(stream, flush, lambda: b.run_async(), args.steps, args.warmup,
+                      after=lambda: kms.append(b.stats()["count_kernel_ms"]))
+    # end to end from pinned host memory: upload + validate all 256, one batched count
+    pinned = [(torch.from_numpy(rp).pin_memory(), torch.from_numpy(cl).pin_memory()) for rp, cl in host]
+    views = [(a.numpy(), c.numpy(), len(a) - 1) for a, c in pinned]
+
+    def e2e_call():
+        assert list(ctx.count_parts_csr(views)) == list(outs)
+
+    e2e_ms = _timed(stream, flush, e2e_call, args.steps, args.warmup)
+    clk = clocks.stop()
+    B_min = B_model = 0
+    for rp, cl in host:
+        bm, bn, _ = _part_bytes(rp, cl, len(rp) - 1)
+        B_model, B_min = B_model + bm, B_min + bn
+    peak, peak_src = _peak()
+    k_ms = sum(kms[args.warmup:]) / max(1, len(kms[args.warmup:]))
+    t0 = time.perf_counter()
+    cpu_total = sum(oracle.count(rp, cl) for rp, cl in host)
+    cpu_s = time.perf_counter() - t0
     kinds = {k: sum(1 for s in specs if s.kind == k) for k in ("er", "chung_lu", "rmat")}
     cfg = {"workload": "uneven_batch_256", "graphs": len(graphs), "kinds": kinds, "oriented_edges": E,
-           "triangles_total": int(outs.sum()), "plain_per_graph_ms": plain_ms, "batched_ms": batch_ms,
-           "speedup": plain_ms / batch_ms, "host_generate_s": gen_s, "device_preprocess_s": prep_s,
-           "largest_graph_edges": max(g.nnz for g in graphs), "smallest_graph_edges": min(g.nnz for g in graphs),
            "l2": "flushed before every timed step (512 MiB memset on the launching stream)"}
+    detail = {"triangles_total": int(outs.sum()), "plain_per_graph_ms": plain_ms, "batched_ms": batch_ms,
+              "speedup": plain_ms / batch_ms, "host_generate_s": gen_s, "device_preprocess_s": prep_s,
+              "largest_graph_edges": max(g.nnz for g in graphs), "smallest_graph_edges": min(g.nnz for g in graphs)}
     res = {"metric": METRIC, "value": world * E / (batch_ms / 1000.0), "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": batch_ms, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-           "data": "synthetic (seeded ER / Chung-Lu / R-MAT mix)", "config": cfg}
+           "data": "synthetic (seeded ER / Chung-Lu / R-MAT mix)", "config": cfg, "detail": detail,
+           "gpu_launches": b.stats()["launches"] * args.steps, "clocks": clk,
+           "e2e": {"value": E / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
+                   "h2d_bytes_per_step": sum(4 * len(rp) + 4 * len(cl) for rp, cl in host),
+                   "d2h_bytes_per_step": 20 * len(host) + 48,
+                   "path": "tc_count_parts_csr_i32 with every row a root: upload + validate 256 graphs, one "
+                           "batched count, read-back"},
+           "roofline": {"bound": "hbm", "achieved": B_min / (k_ms / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": B_min / (k_ms / 1000.0) / 1e9 / peak, "traffic": None,
+                        "peak_source": f"{peak_src} hbm_gbs (copy, burst)",
+                        "kernel": "count_kernel (batched, 256 graphs)", "kernel_ms": k_ms,
+                        "algorithmic_bytes_per_launch": B_min,
+                        "algorithmic_bytes_definition": "sum over graphs of 4(V+1) + 12|E+| + 4 sum_{u->v} "
+                                                        "min(d+(u), d+(v)) + 8",
+                        "survey_model_bytes": B_model,
+                        "survey_model_frac": B_model / (k_ms / 1000.0) / 1e9 / peak},
+           "cpu_baseline": {"value": E / cpu_s, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+                            "sample": "all 256 graphs, one OpenMP count each", "seconds": cpu_s,
+                            "count_matches": cpu_total == int(outs.sum())}}
     b.free()
     ctx.close()
     return res
@@ -894,27 +944,37 @@ def serve_pool(n_graphs: int = 40, seed: int | None = None):
 def run_serve(args, world, rank, local, pg):
     """Serving stream: Poisson arrivals of count requests over a pool of
     graphs; graphs are oriented on the device at admission and kept resident
-    by key (LRU under an 80% HBM budget); latency is submit -> result."""
+    by key (LRU under an 80% HBM budget); latency is submit -> result.
+    Requests of at most 2^20 edges take the small lane, the others the large
+    one; latencies are reported for all requests and per lane."""
     import random
 
-    import torch
-
+    import oracle
     import trianglecount_gb300 as tc
-    torch.cuda.set_device(local)
     ctx = tc.Context(local)
     t0 = time.perf_counter()
     pool = serve_pool()
     gen_s = time.perf_counter() - t0
-    solo, nnz = [], []
+    solo, nnz, host = [], [], []
     for kind, params, (src, dst) in pool:
         g = ctx.graph_from_edges(src, dst)
         solo.append(ctx.count(g))
         nnz.append(g.nnz)
+        host.append(g.download())
         g.free()
+    small_edges = 1 << 20
+    is_small = [len(p[2][0]) <= small_edges for p in pool]
     rates = [float(x) for x in args.rates.split(",")]
     rng = random.Random(0x5EED5E7E)
     sweep = []
-    srv = tc.Server(ctx, hbm_budget_frac=0.8, max_batch=256)
+
+    def pct(v, q):
+        return v[min(len(v) - 1, int(q * len(v)))] if v else None
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    srv = tc.Server(ctx, hbm_budget_frac=0.8, max_batch=256, small_edges=small_edges)
+    h2d = 0
     for rate in rates:
         picks = [rng.randrange(len(pool)) for _ in range(args.requests)]
         gaps = [rng.expovariate(rate) for _ in range(args.requests)]
@@ -928,30 +988,57 @@ def run_serve(args, world, rank, local, pg):
                 time.sleep(dt)
             src, dst = pool[k][2]
             ids.append(srv.submit(src, dst, key=k + 1))
-        lat, edges = [], 0
+            h2d += 16 * len(src)
+        lat, lat_s, lat_l, edges = [], [], [], 0
         for rid, k in zip(ids, picks):
             c, ms = srv.wait(rid)
             assert c == solo[k], "serving result differs from the solo count"
             lat.append(ms)
+            (lat_s if is_small[k] else lat_l).append(ms)
             edges += nnz[k]
         wall = time.perf_counter() - start
         lat.sort()
+        lat_s.sort()
+        lat_l.sort()
         st = srv.stats()
-        sweep.append({"rate_rps": rate, "requests": len(ids), "p50_ms": lat[len(lat) // 2],
-                      "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))], "max_ms": lat[-1],
+        sweep.append({"rate_rps": rate, "requests": len(ids), "p50_ms": pct(lat, 0.5), "p99_ms": pct(lat, 0.99),
+                      "max_ms": lat[-1], "small_p50_ms": pct(lat_s, 0.5), "small_p99_ms": pct(lat_s, 0.99),
+                      "large_p50_ms": pct(lat_l, 0.5), "large_p99_ms": pct(lat_l, 0.99),
+                      "small_requests": len(lat_s), "large_requests": len(lat_l),
                       "achieved_rps": len(ids) / wall, "aggregate_edges_per_s": edges / wall,
-                      "batches_so_far": st["batches"], "cache_hits_so_far": st["cache_hits"],
+                      "batches_so_far": st["batches"], "small_batches_so_far": st["small_batches"],
+                      "large_batches_so_far": st["large_batches"], "cache_hits_so_far": st["cache_hits"],
                       "evictions_so_far": st["evictions"], "max_batch_seen": st["max_batch_seen"]})
     srv.close()
+    clk = clocks.stop()
+    t0 = time.perf_counter()
+    cpu_ok = all(oracle.count(rp, cl) == solo[i] for i, (rp, cl) in enumerate(host))
+    cpu_s = time.perf_counter() - t0
     top = sweep[-1]
+    low = sweep[0]
     cfg = {"workload": "serve_poisson", "pool_graphs": len(pool), "pool_oriented_edges": sum(nnz),
-           "pool_edges_range": [min(nnz), max(nnz)], "sweep": sweep, "host_generate_s": gen_s,
-           "hbm_budget": "80% of device memory", "exact": "every result equals the graph's solo count"}
+           "pool_edges_range": [min(nnz), max(nnz)], "rates_rps": rates, "requests_per_rate": args.requests,
+           "hbm_budget": "80% of device memory", "small_lane": f"requests of at most {small_edges} edges",
+           "exact": "every result equals the graph's solo count"}
     res = {"metric": "serve aggregate oriented edges/s", "value": top["aggregate_edges_per_s"], "unit": UNIT,
            "n_gpus": world, "steps": len(rates), "warmup": 0, "ms_per_step": None, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "int32",
            "data": "synthetic (seeded R-MAT / Chung-Lu pool, Poisson arrivals)", "config": cfg,
-           "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"], "rate_rps": top["rate_rps"]}
+           "detail": {"sweep": sweep, "host_generate_s": gen_s},
+           "p50_ms": low["p50_ms"], "p99_ms": low["p99_ms"], "rate_rps": low["rate_rps"],
+           "p50_p99_note": f"p50 / p99 at the lowest offered rate ({low['rate_rps']:g} req/s); every rate in "
+                           "detail.sweep",
+           "clocks": clk,
+           "e2e": {"value": top["aggregate_edges_per_s"], "unit": UNIT,
+                   "h2d_bytes_per_step": h2d // max(1, len(rates)), "d2h_bytes_per_step": 8 * args.requests,
+                   "path": "tc_server_submit -> tc_server_wait: host edge lists in, counts out (the measurement "
+                           "is end to end by construction)"},
+           "roofline": None,
+           "roofline_note": "a mixed stream of builds and batched counts: the count kernel's roofline is on the "
+                            "rmat23_parts and batch256 lines",
+           "cpu_baseline": {"value": sum(nnz) / cpu_s, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+                            "sample": "every pool graph counted once by the OpenMP oracle", "seconds": cpu_s,
+                            "count_matches": cpu_ok}}
     ctx.close()
     return res
 

@@ -107,9 +107,17 @@ TC_API int tc_ctx_device_info(tc_ctx *ctx, int *sm_count, size_t *free_bytes, si
  * graph none of whose rows is longer (known for uploaded and device-built
  * graphs, not for wrapped ones) is counted by one kernel, one lane per root
  * with N+(u) and each N+(v) in registers -- no transpose, no hash tables
- * (road networks and other bounded-degree graphs).  In
+ * (road networks and other bounded-degree graphs).  intersect selects how a
+ * task's list N+(x) is probed: 0 (default) through the hash tables above;
+ * 1 as the sorted list itself, copied into shared memory as it lies by one
+ * bulk copy (cp.async.bulk, no table to clear or fill) and probed by binary
+ * search (the reference's probe, ShareKernelTCV62_update_v1.cu:12-42), for
+ * light tasks and heavy tiles alike; 2 per light task: the sorted list when
+ * the task's work (probes) is below its list length, so building a table
+ * would cost more than probing it, the hash otherwise (heavy tiles keep the
+ * hash).  hash_pairs = 1 ignores intersect.  In
  * tc_ctx_set_tuning, fields <= 0 (long_list, probe_kicks, heavy_bitmap,
- * blocks_per_sm, hash_pairs, flat_max_deg: < 0) keep the current value. */
+ * blocks_per_sm, hash_pairs, flat_max_deg, intersect: < 0) keep the current value. */
 typedef struct tc_tuning {
     int32_t warp_max_deg;   /* 32..512, power of two */
     int32_t light_max_work; /* wedge probes a light task may have */
@@ -120,16 +128,21 @@ typedef struct tc_tuning {
     int32_t blocks_per_sm;  /* persistent grid = SMs * this (0: occupancy) */
     int32_t hash_pairs;     /* 0 or 1: bucketed-pair hash tables instead of cuckoo / linear */
     int32_t flat_max_deg;   /* 0..8: a graph with no row longer than this counts in one kernel */
+    int32_t intersect;      /* 0: hash tables; 1: sorted lists, bulk-staged; 2: per light task (see above) */
 } tc_tuning;
 TC_API int tc_ctx_get_tuning(tc_ctx *ctx, tc_tuning *out);
 TC_API int tc_ctx_set_tuning(tc_ctx *ctx, const tc_tuning *in);
 /* Autotuner: times the count of g under candidate thresholds (coordinate
  * descent from the current tuning over warp_max_deg, light_max_work,
- * unit_work, long_list, probe_kicks, heavy_bitmap, hash_pairs and
- * flat_max_deg; each candidate the median of `reps` counts; a change is kept
+ * unit_work, long_list, probe_kicks, heavy_bitmap, hash_pairs,
+ * flat_max_deg and intersect; each candidate the median of `reps` counts; a change is kept
  * only if it is at least 2% faster) and sets the fastest on ctx.  best / best_ms may be NULL.  At most max_trials
  * candidates are timed. */
 TC_API int tc_autotune(tc_ctx *ctx, tc_graph *g, int max_trials, int reps, tc_tuning *best, float *best_ms);
+/* tc_autotune that also reports the number of candidates timed (the starting
+ * tuning included; at most max_trials) in *trials (may be NULL). */
+TC_API int tc_autotune_ex(tc_ctx *ctx, tc_graph *g, int max_trials, int reps, tc_tuning *best, float *best_ms,
+                          int *trials);
 
 /* ---- oriented graphs ------------------------------------------------------ */
 /* Upload an oriented CSR: n_rows rows, row_ptr[n_rows+1], col[nnz], rows
@@ -283,27 +296,38 @@ TC_API int tc_halo_extract_ex(tc_ctx *ctx, const tc_ugraph *ug, const int32_t *p
                               tc_graph **parts_out);
 
 /* ---- serving: continuous batching over resident graphs ----------------------- */
-/* No counterpart in the reference (which runs one file per process).  A server
- * owns two contexts on ctx's device: a prep thread admits queued requests by
- * device-memory footprint (evicting least-recently-used idle graphs to stay
- * within the budget) and builds their oriented CSRs on one stream, while a
- * count thread counts every ready request in one batched launch on the other
- * stream; requests arriving during a count are preprocessed concurrently and
- * join the next batch.  Waits are host-side and bounded by batch_timeout_ms;
- * a batch that exceeds it fails with TC_E_TIMEOUT and the server stops
- * admitting. */
+/* No counterpart in the reference (which runs one file per process).  A
+ * server runs two lanes on ctx's device, split by request size (edges given,
+ * or the resident graph's oriented edges): a small lane and a large lane,
+ * each with a prep thread and a count thread on their own two streams (four
+ * contexts).  A prep thread admits its lane's queued requests in arrival
+ * order by device-memory footprint (evicting least-recently-used idle
+ * resident graphs, across both lanes, to stay within the budget) and builds
+ * their oriented CSRs; a count thread counts every ready request of its lane
+ * in one batched launch.  So a large build or a large batch holds up neither
+ * the small requests' builds nor their counts: the small lane's streams have
+ * the higher priority, and the large lane's persistent count kernel leaves
+ * reserve_blocks block slots per SM free for them, so small work runs on
+ * the device beside a large batch.  Requests arriving during a count are
+ * preprocessed concurrently and join their lane's next batch.  Waits are
+ * host-side and bounded by batch_timeout_ms; a batch that exceeds it fails
+ * with TC_E_TIMEOUT and the server stops admitting. */
 typedef struct tc_server_config {
     double hbm_budget_frac;   /* budget = this x device memory (0: 0.8) */
     int64_t hbm_budget_bytes; /* > 0: explicit budget in bytes */
     int32_t max_batch;        /* graphs per batched launch (0: 256) */
     int32_t tie;              /* orientation tie-break of admitted edge lists */
     int32_t batch_timeout_ms; /* watchdog on one batched launch (0: 60000) */
-    int32_t reserved;
+    int32_t reserve_blocks;   /* count-kernel block slots per SM the large lane leaves free (0: 1; < 0: none) */
+    int64_t small_edges;      /* requests with at most this many edges take the small lane (0: 2^20; < 0: one
+                                 lane for all) */
 } tc_server_config;
 
 typedef struct tc_server_stats {
     int64_t submitted, completed, failed, batches, cache_hits, evictions, max_batch_seen;
     int64_t budget_bytes, used_bytes, resident_graphs, queued;
+    int64_t small_batches, large_batches; /* batches taken by each lane's count thread (counted when taken,
+                                              so a batch in flight is already in them and in `batches`) */
 } tc_server_stats;
 
 TC_API int tc_server_create(tc_ctx *ctx, const tc_server_config *cfg, tc_server **out);

@@ -25,6 +25,12 @@ TUNINGS = [
     {"hash_pairs": 1},  # bucketed-pair tables, light and heavy
     {"flat_max_deg": 0},  # bounded-degree graphs through the full chain too
     {"hash_pairs": 1, "warp_max_deg": 32, "light_max_work": 64, "long_list": 5},
+    {"intersect": 1},  # every task on its bulk-staged sorted list (binary search)
+    {"intersect": 1, "warp_max_deg": 32, "light_max_work": 64, "long_list": 0},  # sorted heavy tiles, streamed lists
+    {"intersect": 1, "warp_max_deg": 512, "light_max_work": 1 << 30, "unit_work": 1 << 30, "long_list": 4096},
+    {"intersect": 2},  # per light task: sorted list when its work is below its length
+    {"intersect": 2, "warp_max_deg": 512, "light_max_work": 1 << 30, "long_list": 5},
+    {"intersect": 1, "hash_pairs": 1},  # pair tables ignore intersect
 ]
 
 
@@ -33,7 +39,8 @@ def tuned(ctx):
     old = ctx.get_tuning()
     yield ctx
     ctx.set_tuning(old["warp_max_deg"], old["light_max_work"], old["unit_work"], old["long_list"],
-                   old["probe_kicks"], old["heavy_bitmap"], 0, old["hash_pairs"], old["flat_max_deg"])
+                   old["probe_kicks"], old["heavy_bitmap"], 0, old["hash_pairs"], old["flat_max_deg"],
+                   old["intersect"])
 
 
 @pytest.mark.parametrize("tuning", TUNINGS)
@@ -266,3 +273,21 @@ def test_repeated_counts_on_the_default_stream_and_under_a_caller_capture():
         assert int(out.item()) == want
     g.free()
     c.close()
+
+
+@pytest.mark.parametrize("intersect", [1, 2])
+def test_sorted_lists_on_a_misaligned_wrapped_graph(tuned, intersect):
+    """Wrapped caller arrays need not be 16-byte aligned: the bulk copy is
+    then skipped and the lists are staged by plain loads; counts and per-root
+    counts stay exact."""
+    torch = pytest.importorskip("torch")
+    tuned.set_tuning(intersect=intersect, warp_max_deg=64, light_max_work=256)
+    src, dst = gen.chung_lu(30000, 14.0, seed=5)
+    orp, ocl, want = oracle.pipeline(src, dst)
+    d_rp = torch.from_numpy(orp).cuda()
+    buf = torch.zeros(len(ocl) + 1, dtype=torch.int32, device="cuda")
+    buf[1:] = torch.from_numpy(ocl).cuda()  # col starts 4 bytes past an aligned base
+    g = tuned.wrap_device(d_rp.data_ptr(), buf.data_ptr() + 4, len(orp) - 1, len(ocl))
+    assert tuned.count(g) == want
+    _, want_pr = oracle.count(orp, ocl, per_root=True)
+    assert np.array_equal(tuned.count_per_root(g), want_pr)

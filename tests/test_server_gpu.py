@@ -3,6 +3,7 @@ the same alone and in the mix (exact integers), resident graphs are reused
 by key and evicted LRU under the budget, and the host-side watchdog turns an
 over-long batch into TC_E_TIMEOUT without any device-side fault."""
 import threading
+import time
 
 import numpy as np
 import pytest
@@ -87,3 +88,50 @@ def test_batch_watchdog_reports_timeout(ctx):
         with pytest.raises(tc.TCError) as e:
             srv.wait(srv.submit(*gen.rmat(8)))
         assert e.value.code == "TC_E_STATE"
+
+
+def test_small_requests_overtake_a_large_one_in_flight(ctx):
+    """An R-MAT 22 request (67 M edges, the large lane) is submitted first;
+    once its batch has been taken for counting, small requests (the small
+    lane) arrive.  They are built and counted beside the large batch on their
+    own streams and complete before it; every result equals its solo count."""
+    big = gen.rmat(22)
+    smalls = [gen.rmat(10, seed=300 + i) for i in range(3)] + [gen.chung_lu(5000, 8.0, seed=9)]
+    want_big = oracle.pipeline(*big)[2]
+    want_small = [ctx.count(ctx.graph_from_edges(s, d)) for s, d in smalls]
+    with tc.Server(ctx, max_batch=64) as srv:
+        # warm both lanes (first-use set-up stays out of the race below)
+        srv.wait(srv.submit(*smalls[0]))
+        srv.wait(srv.submit(*gen.rmat(20)))
+        rb = srv.submit(*big, key=77)
+        # wait until the large lane has taken the big batch (its build is done)
+        t_end = time.monotonic() + 60
+        while srv.stats()["large_batches"] < 2 and time.monotonic() < t_end:
+            time.sleep(0.0005)
+        ids = [srv.submit(s, d) for s, d in smalls]
+        order = []
+        pending = set(ids + [rb])
+        t_end = time.monotonic() + 60
+        while pending and time.monotonic() < t_end:
+            for rid in list(pending):
+                r = srv.poll(rid)
+                if r is not None:
+                    order.append((rid, r[0]))
+                    pending.discard(rid)
+            time.sleep(0.0002)
+        st = srv.stats()
+    assert not pending
+    got = dict(order)
+    assert got[rb] == want_big and [got[i] for i in ids] == want_small
+    big_pos = [rid for rid, _ in order].index(rb)
+    assert all([rid for rid, _ in order].index(i) < big_pos for i in ids), order
+    assert st["small_batches"] >= 2 and st["large_batches"] >= 2
+
+
+def test_one_lane_when_small_edges_is_negative(ctx):
+    gs = _graphs()[:3]
+    alone = [ctx.count(ctx.graph_from_edges(s, d)) for s, d in gs]
+    with tc.Server(ctx, small_edges=-1) as srv:
+        got = [srv.wait(srv.submit(s, d))[0] for s, d in gs]
+        st = srv.stats()
+    assert got == alone and st["small_batches"] == 0 and st["large_batches"] >= 1

@@ -68,3 +68,42 @@ def test_contiguous_parts_match_reference_construction():
         for i in range(k):
             ref[i * l:(i + 1) * l] = i
         assert np.array_equal(gen.parts_contig(n, k), ref)
+
+
+def _gpu_rank_main(rank, world, port, k, out_path):
+    """One rank: the library extracts the counting-halo parts on cuda:0 and
+    counts this rank's share in one batched launch; gloo sums the ranks."""
+    import torch.distributed as dist
+
+    import trianglecount_gb300 as tc
+    from trianglecount_gb300.shard import count_sharded
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    with tc.Context(0) as ctx:
+        ug = ctx.ugraph_from_edges(*gen.rmat(14))
+        parts = ctx.halo_extract(ug, gen.parts_random(ug.info()[0], k), k, mode="count")
+        mine = assign_parts([p.nnz for p in parts], world)[rank]
+        outs = ctx.batch([parts[i] for i in mine]).run() if mine else []
+        by_part = dict(zip(mine, (int(x) for x in outs)))
+        total = count_sharded(parts, rank, world, lambda p: by_part[parts.index(p)])
+    with open(f"{out_path}.{rank}", "w") as f:
+        f.write(f"{total} {len(mine)}")
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("k", [3, 8])
+def test_two_gloo_ranks_count_parts_on_the_gpu(tmp_path, k):
+    """Two processes share cuda:0 (their kernels never wait on each other):
+    each counts its LPT share of the parts with libtc, and the gloo sum
+    equals the oracle's count of the whole graph."""
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    out = str(tmp_path / "gpu_total")
+    mp.start_processes(_gpu_rank_main, args=(2, _free_port(), k, out), nprocs=2, join=True, start_method="spawn")
+    whole = oracle.pipeline(*gen.rmat(14))[2]
+    res = [open(f"{out}.{r}").read().split() for r in range(2)]
+    assert [int(t) for t, _ in res] == [whole, whole]
+    assert sum(int(n) for _, n in res) == k

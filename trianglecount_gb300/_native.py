@@ -33,7 +33,7 @@ class Tuning(C.Structure):
     _fields_ = [("warp_max_deg", C.c_int32), ("light_max_work", C.c_int32), ("unit_work", C.c_int32),
                 ("long_list", C.c_int32), ("probe_kicks", C.c_int32), ("heavy_bitmap", C.c_int32),
                 ("blocks_per_sm", C.c_int32), ("hash_pairs", C.c_int32),
-                ("flat_max_deg", C.c_int32)]
+                ("flat_max_deg", C.c_int32), ("intersect", C.c_int32)]
 
 
 class CountStats(C.Structure):
@@ -43,13 +43,14 @@ class CountStats(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_frac", C.c_double), ("hbm_budget_bytes", C.c_int64), ("max_batch", C.c_int32),
-                ("tie", C.c_int32), ("batch_timeout_ms", C.c_int32), ("reserved", C.c_int32)]
+                ("tie", C.c_int32), ("batch_timeout_ms", C.c_int32), ("reserve_blocks", C.c_int32),
+                ("small_edges", C.c_int64)]
 
 
 class ServerStats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "failed", "batches", "cache_hits", "evictions",
                                          "max_batch_seen", "budget_bytes", "used_bytes", "resident_graphs",
-                                         "queued")]
+                                         "queued", "small_batches", "large_batches")]
 
 
 vp = C.c_void_p
@@ -73,6 +74,7 @@ _SIGS = {
     "tc_ctx_get_tuning": (C.c_int, [vp, P(Tuning)]),
     "tc_ctx_set_tuning": (C.c_int, [vp, P(Tuning)]),
     "tc_autotune": (C.c_int, [vp, vp, C.c_int, C.c_int, P(Tuning), P(C.c_float)]),
+    "tc_autotune_ex": (C.c_int, [vp, vp, C.c_int, C.c_int, P(Tuning), P(C.c_float), P(C.c_int)]),
     "tc_graph_upload_i32": (C.c_int, [vp, vp, vp, i64, i64, i64, P(vp)]),
     "tc_graph_upload_u64": (C.c_int, [vp, vp, vp, i64, i64, i64, P(vp)]),
     "tc_graph_wrap_device_i32": (C.c_int, [vp, vp, vp, i64, i64, i64, P(vp)]),

@@ -166,8 +166,13 @@ class Server:
     """Continuous-batching triangle-count server (tc_server_* in the C ABI)."""
 
     def __init__(self, ctx: "Context", hbm_budget_frac: float = 0.8, hbm_budget_bytes: int = 0,
-                 max_batch: int = 256, tie="reference", batch_timeout_ms: int = 60000):
-        cfg = N.ServerConfig(hbm_budget_frac, hbm_budget_bytes, max_batch, _tie(tie), batch_timeout_ms, 0)
+                 max_batch: int = 256, tie="reference", batch_timeout_ms: int = 60000, reserve_blocks: int = 0,
+                 small_edges: int = 0):
+        """small_edges: requests with at most this many edges take the small
+        lane (0: 2^20, < 0: one lane); reserve_blocks: count-kernel block slots
+        per SM the large lane leaves to the small one (0: 1, < 0: none)."""
+        cfg = N.ServerConfig(hbm_budget_frac, hbm_budget_bytes, max_batch, _tie(tie), batch_timeout_ms,
+                             reserve_blocks, small_edges)
         h = C.c_void_p()
         N.call("tc_server_create", ctx.handle, C.byref(cfg), C.byref(h))
         self._h = h
@@ -280,19 +285,30 @@ class Context:
 
     def set_tuning(self, warp_max_deg: int = 0, light_max_work: int = 0, unit_work: int = 0, long_list: int = -1,
                    probe_kicks: int = -1, heavy_bitmap: int = -1, blocks_per_sm: int = -1,
-                   hash_pairs: int = -1, flat_max_deg: int = -1) -> None:
+                   hash_pairs: int = -1, flat_max_deg: int = -1, intersect: int = -1) -> None:
         t = N.Tuning(warp_max_deg, light_max_work, unit_work, long_list, probe_kicks, heavy_bitmap, blocks_per_sm,
-                     hash_pairs, flat_max_deg)
+                     hash_pairs, flat_max_deg, intersect)
         N.call("tc_ctx_set_tuning", self._h, C.byref(t))
 
-    def autotune(self, g: "Graph", max_trials: int = 32, reps: int = 3) -> tuple[dict, float]:
-        """Picks the fastest strategy thresholds for g by timing (sets them)."""
+    def autotune(self, g: "Graph", max_trials: int = 32, reps: int = 3, with_trials: bool = False):
+        """Picks the fastest strategy thresholds for g by timing (sets them);
+        returns (tuning, best ms) or, with_trials, (tuning, best ms, trials)."""
         t = N.Tuning()
         ms = C.c_float()
-        N.call("tc_autotune", self._h, g.handle, int(max_trials), int(reps), C.byref(t), C.byref(ms))
-        return {k: getattr(t, k) for k, _ in N.Tuning._fields_}, ms.value
+        n = C.c_int()
+        N.call("tc_autotune_ex", self._h, g.handle, int(max_trials), int(reps), C.byref(t), C.byref(ms), C.byref(n))
+        tun = {k: getattr(t, k) for k, _ in N.Tuning._fields_}
+        return (tun, ms.value, n.value) if with_trials else (tun, ms.value)
 
     # ---- graphs ----
+    def wrap_device(self, d_row_ptr: int, d_col: int, n_rows: int, nnz: int, n_roots: int | None = None) -> Graph:
+        """A graph over caller-owned int32 device arrays (addresses), not copied
+        and not validated; the caller keeps them alive."""
+        h = C.c_void_p()
+        N.call("tc_graph_wrap_device_i32", self._h, C.c_void_p(d_row_ptr), C.c_void_p(d_col), int(n_rows), int(nnz),
+               int(n_rows if n_roots is None else n_roots), C.byref(h))
+        return Graph(self, h)
+
     def upload(self, row_ptr: np.ndarray, col: np.ndarray, n_roots: int | None = None) -> Graph:
         """Upload an oriented CSR (int32, or u64 narrowed on the device)."""
         n_rows = len(row_ptr) - 1

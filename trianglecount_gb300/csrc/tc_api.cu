@@ -151,6 +151,11 @@ int ensure_count_scratch(tc_graph *g) {
 
 __global__ void set_desc_kernel(GraphDesc *dst, GraphDesc d) { *dst = d; }
 
+// The count kernels' error word (CountWork::error) as text.
+const char *count_error_text(int code) {
+    return code == 2 ? "a bulk-copy staging wait of the count kernel gave up" : "heavy-unit list overflow";
+}
+
 // A stream the library may capture: not a default stream (those cannot be
 // captured) and not one the caller is capturing (the chain's launches then
 // belong to the caller's graph).
@@ -459,7 +464,7 @@ int count_graphs_direct(tc_ctx *ctx, tc_graph *const *graphs, int n, uint64_t *o
     }
     if (st == TC_OK) {
         const CountWork *w = (const CountWork *)h_out;
-        if (w->error) st = set_error(TC_E_STATE, "heavy-unit list overflow");
+        if (w->error) st = set_error(TC_E_STATE, "%s", count_error_text(w->error));
         else memcpy(outs, h_out + sizeof(CountWork), sizeof(uint64_t) * (size_t)n);
         if (kernel_ms) cudaEventElapsedTime(kernel_ms, ctx->ev[0], ctx->ev[1]);
     }
@@ -572,6 +577,7 @@ int tc_ctx_create(int device, tc_ctx **out) {
     c->tuning.blocks_per_sm = 0;
     c->tuning.hash_pairs = 0;
     c->tuning.flat_max_deg = 8;
+    c->tuning.intersect = 0;
     int st = TC_OK;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) st = TC_E_CUDA;
     c->own_stream = true;
@@ -651,6 +657,7 @@ int tc_ctx_set_tuning(tc_ctx *c, const tc_tuning *in) {
     if (in->blocks_per_sm >= 0) t.blocks_per_sm = in->blocks_per_sm;
     if (in->hash_pairs >= 0) t.hash_pairs = in->hash_pairs;
     if (in->flat_max_deg >= 0) t.flat_max_deg = in->flat_max_deg;
+    if (in->intersect >= 0) t.intersect = in->intersect;
     Tuned r;
     TC_TRY(resolve_tuning(t, c->sm_count, &r));
     c->tuning = t;
@@ -790,7 +797,7 @@ int tc_count(tc_ctx *ctx, tc_graph *g, uint64_t *out, tc_count_stats *stats) {
     TC_CUDA(cudaEventRecord(ctx->ev[2], s));
     TC_CUDA(cudaStreamSynchronize(s));
     const CountWork *w = (const CountWork *)ctx->h_pinned;
-    if (w->error) return set_error(TC_E_STATE, "heavy-unit list overflow");
+    if (w->error) return set_error(TC_E_STATE, "%s", count_error_text(w->error));
     *out = *(const unsigned long long *)(w + 1);
     if (stats) {
         TC_CUDA(cudaEventElapsedTime(&stats->count_ms, ctx->ev[0], ctx->ev[1]));
@@ -822,7 +829,8 @@ int tc_count_per_root(tc_ctx *ctx, tc_graph *g, uint64_t *per_root, uint64_t *to
                                 cudaMemcpyDeviceToHost, s));
     TC_CUDA(cudaMemcpyAsync(ctx->h_pinned, g->d_work, sizeof(CountWork), cudaMemcpyDeviceToHost, s));
     TC_CUDA(cudaStreamSynchronize(s));
-    if (((const CountWork *)ctx->h_pinned)->error) return set_error(TC_E_STATE, "heavy-unit list overflow");
+    if (((const CountWork *)ctx->h_pinned)->error)
+        return set_error(TC_E_STATE, "%s", count_error_text(((const CountWork *)ctx->h_pinned)->error));
     if (total) {
         uint64_t t = 0;
         for (int64_t u = 0; u < g->n_roots; ++u) t += per_root[u];
@@ -999,7 +1007,7 @@ int tc_batch_results(tc_batch *b, uint64_t *outs) {
                             cudaMemcpyDeviceToHost, s));
     TC_CUDA(cudaStreamSynchronize(s));
     const CountWork *w = (const CountWork *)b->h_out;
-    if (w->error) return set_error(TC_E_STATE, "heavy-unit list overflow");
+    if (w->error) return set_error(TC_E_STATE, "%s", count_error_text(w->error));
     memcpy(outs, (const void *)(w + 1), sizeof(uint64_t) * (size_t)b->n);
     return TC_OK;
 }

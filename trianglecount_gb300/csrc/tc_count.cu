@@ -203,14 +203,126 @@ __device__ __forceinline__ uint32_t bitmap_probe(const int *bm, int x) {
     return ((uint32_t)bm[(unsigned)y >> 5] >> (y & 31)) & (uint32_t)(x >= 0);
 }
 
-// Table modes, chosen per table (warp- or block-uniform).
-constexpr int kLinear = 0, kCuckoo = 1, kPairs = 2;
+// Table modes, chosen per table (warp- or block-uniform).  kSorted is not a
+// hash: the task's list itself, staged in shared memory as it lies (sorted),
+// probed by binary search.
+constexpr int kLinear = 0, kCuckoo = 1, kPairs = 2, kSorted = 3;
+
+// ---- bulk staging of a sorted list into shared memory ------------------------
+// A list col[s, s + n) is copied into a 16-byte-aligned shared buffer by one
+// cp.async.bulk (the Blackwell/Hopper bulk-copy engine, no registers or
+// load instructions per element), completing on an mbarrier.  The copy covers
+// the 16-byte-aligned span [s & ~3, ceil4(s + n)) of col, clamped below
+// floor4(nnz) so it never reads past the array; the few elements past the
+// clamp (only at the end of col) are loaded by plain loads.  Element i of the
+// list is then buf[o + i], o = s - (s & ~3).  A col that is not 16-byte
+// aligned (a wrapped caller array) is staged by plain loads only.
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// Orders this thread's earlier generic-proxy shared accesses before later
+// async-proxy (bulk copy) writes to the same addresses.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, unsigned long long *bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Waits for the barrier's phase `parity` to complete, at most kWaitRounds
+// try_wait calls (each suspends for a bounded, hardware-chosen time); false
+// when it gave up.  A bulk copy of a few KB completes in microseconds, so a
+// give-up means a broken invariant, which the caller reports as an error.
+constexpr int kWaitRounds = 1 << 22;
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t parity) {
+    for (int it = 0; it < kWaitRounds; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// Bytes the bulk part of staging col[s, s + n) copies (0: none); every
+// thread of the staging group computes it, one issues the copy.
+__device__ __forceinline__ uint32_t stage_bytes(const int32_t *col, int64_t lim4, int s, int n) {
+    if (((uintptr_t)col & 15u) != 0) return 0;
+    const int64_t a0 = s & ~3;
+    int64_t a1 = ((int64_t)s + n + 3) & ~(int64_t)3;
+    if (a1 > lim4) a1 = lim4;
+    return a1 > a0 ? (uint32_t)(a1 - a0) * 4u : 0u;
+}
+
+// Issues the staging of col[s, s + n) into buf (16-byte aligned) by one
+// thread (the caller's elected thread) and returns the bulk part's byte
+// count (0: nothing issued, no barrier phase used).  lim4 = floor4(nnz).
+__device__ __forceinline__ uint32_t stage_issue(const int32_t *col, int64_t lim4, int s, int n, int *buf,
+                                                unsigned long long *bar) {
+    if (((uintptr_t)col & 15u) != 0) return 0;
+    const int64_t a0 = s & ~3;
+    int64_t a1 = ((int64_t)s + n + 3) & ~(int64_t)3;
+    if (a1 > lim4) a1 = lim4;
+    if (a1 <= a0) return 0;
+    const uint32_t bytes = (uint32_t)(a1 - a0) * 4u;
+    bulk_load(buf, col + a0, bytes, bar);
+    return bytes;
+}
+
+// The elements of col[s, s + n) that the bulk part does not cover, by plain
+// loads; threads tid, tid + nthreads, ...
+// Returns whether any element was written this way (the same on every thread).
+__device__ __forceinline__ bool stage_rest(const int32_t *col, int64_t lim4, int s, int n, int *buf, int tid,
+                                           int nthreads) {
+    int64_t first = s;  // the first element the bulk part does not cover
+    if (((uintptr_t)col & 15u) == 0) {
+        int64_t a1 = ((int64_t)s + n + 3) & ~(int64_t)3;
+        if (a1 > lim4) a1 = lim4;
+        if (a1 > (int64_t)(s & ~3) && a1 > first) first = a1;
+    }
+    const int o = s & 3;
+    for (int64_t j = first + tid; j < (int64_t)s + n; j += nthreads) buf[o + (int)(j - s)] = __ldg(col + j);
+    return first < (int64_t)s + n;
+}
+
+// Membership of x in the sorted list a[0, n) (n >= 1) by a branch-free binary
+// search: ceil(log2 n) dependent shared loads, the same count on every lane
+// of a warp probing one list (the reference's Search on a shared tile,
+// ShareKernelTCV62_update_v1.cu:12-42, on the whole list instead of 128-entry
+// tiles).
+__device__ __forceinline__ uint32_t sorted_probe(const int *a, int n, int x) {
+    int lo = 0;
+    for (int len = n; len > 1;) {
+        const int half = len >> 1;
+        lo = a[lo + half] <= x ? lo + half : lo;
+        len -= half;
+    }
+    return (uint32_t)(a[lo] == x);
+}
 
 // Membership of x >= 0 in the table, by the table's mode (kPairsOnly: the
 // kernel instance that builds pair tables only).
 template <bool kPairsOnly>
 __device__ __forceinline__ uint32_t probe_any(const int *tab, uint32_t mask, int shift, int x, int mode) {
     if (kPairsOnly) return pair_probe(tab, mask >> 1, shift, x);
+    if (mode == kSorted) return sorted_probe(tab, (int)mask, x);  // mask = the list's length
     return mode == kCuckoo ? cuckoo_probe(tab, shift, x) : table_probe(tab, mask, shift, x);
 }
 
@@ -282,6 +394,8 @@ struct KParams {
     int probe_kicks;  // 0: linear probing; > 0: cuckoo with this many kicks
     int table_mode;   // preferred table mode: kPairs, kCuckoo (probe_kicks > 0) or kLinear
     int heavy_done;   // heavy units belong to heavy_bitmap_kernel: count_kernel skips phase A
+    int intersect;    // 0: hash tables; 1: every task on its bulk-staged sorted list (binary search);
+                      // 2: per light task, the sorted list when its work is below its list length
     int aux_dynamic;  // auxiliary kernels walk chunks from cursors (batches) instead of grid-stride
     int count_blocks; // persistent grid of count_kernel
 };
@@ -358,6 +472,9 @@ __device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ r
             } else if (mode == kCuckoo) {
 #pragma unroll
                 for (int i = 0; i < 4; ++i) h += (uint32_t)(x[i] >= 0) & cuckoo_probe(tab, shift, x[i]);
+            } else if (mode == kSorted) {  // four independent searches in flight
+#pragma unroll
+                for (int i = 0; i < 4; ++i) h += (uint32_t)(x[i] >= 0) & sorted_probe(tab, (int)mask, x[i]);
             } else {
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
@@ -988,12 +1105,13 @@ __global__ void __launch_bounds__(kBigThreads, 1) heavy_bitmap_kernel(KParams P,
     }
 }
 
-template <bool kPerRoot, bool kPairsOnly>
+template <bool kPerRoot, bool kPairsOnly, bool kStage = false>
 __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KParams P) {
-    extern __shared__ int smem[];
+    extern __shared__ __align__(16) int smem[];
     __shared__ unsigned s_unit;
     __shared__ int s_entry;
     __shared__ int s_chunk;
+    __shared__ __align__(8) unsigned long long s_bar[kWarpsPerBlock + 1];  // bulk-copy barriers: per warp, block
     const int lane = threadIdx.x & (kWarp - 1);
     const int warp = threadIdx.x / kWarp;
 
@@ -1010,10 +1128,24 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
     const unsigned long long packed = P.work->heavy_packed;
     const unsigned n_entries = (unsigned)min((unsigned long long)(packed >> 32), (unsigned long long)P.heavy_cap);
     const unsigned n_units = (unsigned)(packed & 0xffffffffull);
+    // sorted-list tasks stage their list with bulk copies (uniform: a kernel parameter)
+    const bool staging = kStage && !kPairsOnly && P.intersect != 0;
+    uint32_t bphase = 0, wphase = 0;  // parity of the block's and this warp's barrier
+    bool stage_ok = true;
+    // The block's (warp's) shared region was last written by generic stores
+    // (a hash table, or the plain-load part of a staged list): a bulk copy over
+    // it must first be ordered after them by a proxy fence.
+    bool block_dirty = false, warp_dirty = false;
+    if (staging) {
+        if (threadIdx.x <= kWarpsPerBlock) mbar_init(&s_bar[threadIdx.x], 1);
+        mbar_fence_init();
+        __syncthreads();
+    }
 
     // ---- phase A: heavy units, one block each ----
     int cached_entry = -1, cached_tile = -1;
     int cached_mode = kLinear;
+    const int *cached_tab = smem;
     for (; !P.heavy_done;) {
         if (warp == 0) {
             unsigned unit = 0;
@@ -1067,32 +1199,66 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
         const uint32_t mask = (1u << lg) - 1u;
         const int shift = 32 - lg;
         if (ei != cached_entry || ti != cached_tile) {
-            table_clear(smem, mask, threadIdx.x, kThreads);
-            __syncthreads();
-            bool ok = true;
-            cached_mode = table_fill<kPairsOnly>(smem, mask, shift, col + rs + t0, tl, threadIdx.x, kThreads,
-                                                 P.table_mode, P.probe_kicks, &ok);
-            if (__syncthreads_or(!ok)) {  // a cuckoo give-up: linear probing instead
+            if (staging && P.intersect == 1) {
+                // the tile as it lies (sorted) by one bulk copy: no clear, no inserts
+                const int64_t lim4 = (int64_t)__ldg(rp + G.n_rows) & ~(int64_t)3;
+                const uint32_t bytes = stage_bytes(col, lim4, rs + t0, tl);
+                if (bytes && block_dirty) {
+                    fence_proxy_async();
+                    __syncthreads();
+                }
+                if (threadIdx.x == 0 && bytes) stage_issue(col, lim4, rs + t0, tl, smem, &s_bar[kWarpsPerBlock]);
+                block_dirty = stage_rest(col, lim4, rs + t0, tl, smem, threadIdx.x, kThreads);
+                if (bytes) {
+                    if (!mbar_wait(&s_bar[kWarpsPerBlock], bphase)) {
+                        stage_ok = false;
+                        mbar_wait(&s_bar[kWarpsPerBlock], bphase);  // the copy in flight, bounded again
+                    }
+                    bphase ^= 1u;
+                }
+                cached_mode = kSorted;
+                cached_tab = smem + ((rs + t0) & 3);
+            } else {
                 table_clear(smem, mask, threadIdx.x, kThreads);
                 __syncthreads();
-                cached_mode = table_fill<false>(smem, mask, shift, col + rs + t0, tl, threadIdx.x, kThreads, kLinear, 0,
-                                                &ok);
+                bool ok = true;
+                cached_mode = table_fill<kPairsOnly>(smem, mask, shift, col + rs + t0, tl, threadIdx.x, kThreads,
+                                                     P.table_mode, P.probe_kicks, &ok);
+                if (__syncthreads_or(!ok)) {  // a cuckoo give-up: linear probing instead
+                    table_clear(smem, mask, threadIdx.x, kThreads);
+                    __syncthreads();
+                    cached_mode = table_fill<false>(smem, mask, shift, col + rs + t0, tl, threadIdx.x, kThreads,
+                                                    kLinear, 0, &ok);
+                }
+                cached_tab = smem;
+                block_dirty = true;
             }
             cached_entry = ei;
             cached_tile = ti;
         }
+        if (staging && __syncthreads_or(!stage_ok)) {  // a staging wait gave up: report, stop
+            if (threadIdx.x == 0) atomicExch(&P.work->error, 2);
+            return;
+        }
         __syncthreads();
         const int per = (n_part + ns - 1) / ns;
         const int j0 = si * per, j1 = min(n_part, j0 + per);
+        const uint32_t pmask = cached_mode == kSorted ? (uint32_t)tl : mask;
+        // partners per grab: kHeavyChunk, or fewer when the unit has fewer than
+        // kHeavyChunk partners per warp, so that every warp gets a grab (a hub's
+        // unit in a halo part holds only that part's in-partners: at 16 per
+        // grab most warps would wait at the barrier below)
+        const int chunk = max(1, min(kHeavyChunk, (j1 - j0 + kWarpsPerBlock - 1) / kWarpsPerBlock));
         uint32_t hits = 0;
         for (;;) {
             int c = 0;
             if (lane == 0) c = atomicAdd(&s_chunk, 1);
             c = __shfl_sync(kFull, c, 0);
-            const int jb = j0 + c * kHeavyChunk;
+            const int jb = j0 + c * chunk;
             if (jb >= j1) break;
-            hits += probe_partners<kPerRoot, false, kPairsOnly>(rp, col, T, jb, min(jb + kHeavyChunk, j1), smem, mask, shift,
-                                             cached_mode, P.long_list, lane, G.per_root);
+            hits += probe_partners<kPerRoot, false, kPairsOnly>(rp, col, T, jb, min(jb + chunk, j1), cached_tab,
+                                                                pmask, shift, cached_mode, P.long_list, lane,
+                                                                G.per_root);
         }
         if (!kPerRoot) {
             if (e.g != cur_g) flush(e.g);
@@ -1100,6 +1266,7 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
         }
         __syncthreads();
     }
+    warp_dirty = block_dirty;  // the warp regions lie in the block's region
 
     // ---- phase B: light tasks, one warp each ----
     // Warps take kLightGrab tasks at a time from the classifier's list, so the
@@ -1114,6 +1281,7 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
         const int nt = (int)min((unsigned)kLightGrab, n_light - t0);
         // the grabbed tasks' rows, one lane each
         int rs = 0, d = 0, i0 = 0, i1 = 0, tg = 0, tx = 0;
+        unsigned long long tw = 0;  // the task's work (probes), for the per-task switch
         if (lane < nt) {
             const uint32_t gi = P.light_list[t0 + lane];
             const int64_t c = (int64_t)(gi / kWarp);
@@ -1124,6 +1292,8 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
             d = __ldg(Gl.rp + tx + 1) - rs;
             i0 = P.in_off[Gl.vbase + tx];
             i1 = P.in_off[Gl.vbase + tx + 1];
+            if (staging && P.intersect == 2)
+                tw = P.out_work[Gl.vbase + tx] + (P.in_work[Gl.vbase + tx] & 0xffffffffull);
         }
         for (int k = 0; k < nt; ++k) {
             const int g = __shfl_sync(kFull, tg, k);
@@ -1141,25 +1311,55 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
             T.in_nbr = P.in_list + ri0;
             const int n_part = T.n_out + (__shfl_sync(kFull, i1, k) - ri0);
             const int lg = table_log_slots(T.dx);
-            const uint32_t mask = (1u << lg) - 1u;
+            uint32_t mask = (1u << lg) - 1u;
             const int shift = 32 - lg;
-            table_clear(wtab, mask, lane, kWarp);
-            __syncwarp();
-            bool ok = true;
-            int mode = table_fill<kPairsOnly>(wtab, mask, shift, col + rrs, T.dx, lane, kWarp, P.table_mode,
-                                              P.probe_kicks, &ok);
-            if (!__all_sync(kFull, ok)) {  // a cuckoo give-up: linear probing instead
-                __syncwarp();
+            int mode;
+            const int *tab = wtab;
+            const unsigned long long task_w = __shfl_sync(kFull, tw, k);
+            if (staging && (P.intersect == 1 || task_w < (unsigned long long)T.dx)) {
+                // few probes for the list's length (or every task): the list as it
+                // lies, bulk-copied, instead of a table built for it
+                const int64_t lim4 = (int64_t)__ldg(rp + G.n_rows) & ~(int64_t)3;
+                const uint32_t bytes = stage_bytes(col, lim4, rrs, T.dx);
+                if (bytes && warp_dirty) {
+                    fence_proxy_async();
+                    __syncwarp();
+                }
+                if (lane == 0 && bytes) stage_issue(col, lim4, rrs, T.dx, wtab, &s_bar[warp]);
+                warp_dirty = stage_rest(col, lim4, rrs, T.dx, wtab, lane, kWarp);
+                if (bytes) {
+                    if (!mbar_wait(&s_bar[warp], wphase)) {
+                        stage_ok = false;
+                        mbar_wait(&s_bar[warp], wphase);  // the copy in flight, bounded again
+                    }
+                    wphase ^= 1u;
+                }
+                mode = kSorted;
+                tab = wtab + (rrs & 3);
+                mask = (uint32_t)T.dx;
+            } else {
                 table_clear(wtab, mask, lane, kWarp);
                 __syncwarp();
-                mode = table_fill<false>(wtab, mask, shift, col + rrs, T.dx, lane, kWarp, kLinear, 0, &ok);
+                bool ok = true;
+                mode = table_fill<kPairsOnly>(wtab, mask, shift, col + rrs, T.dx, lane, kWarp, P.table_mode,
+                                              P.probe_kicks, &ok);
+                if (!__all_sync(kFull, ok)) {  // a cuckoo give-up: linear probing instead
+                    __syncwarp();
+                    table_clear(wtab, mask, lane, kWarp);
+                    __syncwarp();
+                    mode = table_fill<false>(wtab, mask, shift, col + rrs, T.dx, lane, kWarp, kLinear, 0, &ok);
+                }
+                warp_dirty = true;
+            }
+            if (staging && __any_sync(kFull, !stage_ok)) {  // a staging wait gave up: report, stop
+                if (lane == 0) atomicExch(&P.work->error, 2);
+                return;
             }
             __syncwarp();
             uint32_t hits = 0;
             for (int jb = 0; jb < n_part; jb += kWarp)
-                hits += probe_partners<kPerRoot, false, kPairsOnly>(rp, col, T, jb, min(jb + kWarp, n_part), wtab, mask,
-                                                                    shift, mode,
-                                                 P.long_list, lane, G.per_root);
+                hits += probe_partners<kPerRoot, false, kPairsOnly>(rp, col, T, jb, min(jb + kWarp, n_part), tab, mask,
+                                                                    shift, mode, P.long_list, lane, G.per_root);
             __syncwarp();
             if (!kPerRoot) acc += hits;
         }
@@ -1194,6 +1394,8 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     r.hash_pairs = t.hash_pairs >= 0 ? t.hash_pairs : 0;
     if (r.hash_pairs > 1) return set_error(TC_E_INVALID, "hash_pairs must be 0 or 1, got %d", r.hash_pairs);
     r.flat_max_deg = t.flat_max_deg >= 0 ? t.flat_max_deg : 8;
+    r.intersect = t.intersect >= 0 ? t.intersect : 0;
+    if (r.intersect > 2) return set_error(TC_E_INVALID, "intersect must be 0, 1 or 2, got %d", r.intersect);
     if (r.flat_max_deg > kMicroDeg)
         return set_error(TC_E_INVALID, "flat_max_deg must be in [0, %d], got %d", kMicroDeg, r.flat_max_deg);
     r.sm_count = sm_count;
@@ -1218,6 +1420,10 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     TC_CUDA(cudaFuncSetAttribute(count_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
     TC_CUDA(cudaFuncSetAttribute(count_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
     TC_CUDA(cudaFuncSetAttribute(count_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
+    TC_CUDA(cudaFuncSetAttribute(count_kernel<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)r.smem));
+    TC_CUDA(cudaFuncSetAttribute(count_kernel<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)r.smem));
     int occ = 0;
     TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, count_kernel<false, false>, kThreads, r.smem));
     if (occ < 1) return set_error(TC_E_INVALID, "count kernel does not fit on an SM with %zu B shared memory", r.smem);
@@ -1280,6 +1486,7 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
     P.probe_kicks = tn.probe_kicks;
     P.table_mode = tn.hash_pairs ? kPairs : tn.probe_kicks > 0 ? kCuckoo : kLinear;
     P.count_blocks = tn.blocks;
+    P.intersect = tn.hash_pairs ? 0 : tn.intersect;  // the pair-table instance has no sorted mode
     // heavy units on direct-address bitmaps when every graph's ids fit in shared memory
     const int64_t bitmap_words = (max_rows + 31) / 32;
     const bool bitmap = tn.heavy_bitmap && bitmap_words > 0 && bitmap_words * 4 <= (int64_t)tn.bitmap_bytes;
@@ -1320,9 +1527,11 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
         }
         if (per_root) {
             if (tn.hash_pairs) count_kernel<true, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+            else if (P.intersect) count_kernel<true, false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
             else count_kernel<true, false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
         } else {
             if (tn.hash_pairs) count_kernel<false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+            else if (P.intersect) count_kernel<false, false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
             else count_kernel<false, false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
         }
         if (kev) TC_TRY(record_kernel_event(kev[1], s));
@@ -1391,6 +1600,7 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
     P.table_mode = tn.hash_pairs ? kPairs : tn.probe_kicks > 0 ? kCuckoo : kLinear;
     P.count_blocks = tn.blocks;
     P.heavy_done = 0;
+    P.intersect = 0;
     TC_CUDA(cudaMemsetAsync(work, 0, sizeof(CountWork), s));
     TC_CUDA(cudaMemsetAsync(results, 0, sizeof(unsigned long long), s));
     if (total_chunks > 0) {

@@ -102,7 +102,7 @@ struct CountWork {
     unsigned int heavy_cursor;
     unsigned int small_cursor;       // light-task cursor
     unsigned int aux_cursor[2];      // chunk cursors of in_count, transpose/classify
-    int error;
+    int error;                       // 1: heavy-unit list overflow; 2: a bulk-copy staging wait gave up
     unsigned long long total_work;   // sum over oriented edges of the cheaper side's length
     unsigned long long n_tasks;      // tasks listed by the classifier, one atomic per chunk for both
                                      // lists: light (low half, task list from the bottom) and micro
@@ -119,6 +119,7 @@ struct Tuned {  // resolved tc_tuning with derived table geometry
     int heavy_bitmap;    // 1: heavy units on direct-address bitmaps when the ids fit
     int hash_pairs;      // 1: bucketed-pair hash tables (one 8-byte load per probe)
     int flat_max_deg;    // graphs whose rows are all this short count with flat_kernel (0: never)
+    int intersect;       // 0: hash tables; 1: bulk-staged sorted lists; 2: per light task by its work
     int bitmap_bytes;    // shared memory the bitmap kernel may use (ids < 8 x this)
     int sm_count;
     int tile;            // block table entries per tile (a quarter of its slots)

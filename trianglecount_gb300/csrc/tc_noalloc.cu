@@ -96,6 +96,7 @@ int setup_device(int dev, DeviceSetup **out) {
         t.blocks_per_sm = 0;
         t.hash_pairs = 0;
         t.flat_max_deg = 0;  // the flat count is not used here
+        t.intersect = 0;
         TC_TRY(resolve_tuning(t, device_sm_count(dev), &d.tuned));
         d.scratch = (unsigned char *)p;
         d.ready = true;

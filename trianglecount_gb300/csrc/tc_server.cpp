@@ -1,19 +1,27 @@
 // tc_server.cpp -- continuous-batching request loop for triangle counts.
 //
 // Requests carry an edge list (or only the key of a graph already resident).
-// Two host threads drive one device through two contexts (two streams):
+// They are split by size into two lanes, small and large, each driven by two
+// host threads on their own contexts (streams) of one device:
 //
-//   prep thread   takes queued requests in arrival order, admits each when its
-//                 footprint fits the HBM budget (evicting least-recently-used
-//                 idle resident graphs when needed), and builds the oriented CSR
-//                 on the device (clean-up + orientation on the prep stream);
-//                 the graph stays resident under its key for later requests.
-//   count thread  takes every ready request (up to max_batch), counts all their
-//                 graphs with one batched persistent launch on the count stream,
-//                 and completes the requests.
+//   prep thread   takes its lane's queued requests in arrival order, admits
+//                 each when its footprint fits the HBM budget shared by both
+//                 lanes (evicting least-recently-used idle resident graphs when
+//                 needed), and builds the oriented CSR on the device (clean-up +
+//                 orientation on the lane's prep stream); the graph stays
+//                 resident under its key for later requests.
+//   count thread  takes every ready request of its lane (up to max_batch),
+//                 counts all their graphs with one batched persistent launch on
+//                 the lane's count stream, and completes the requests.
 //
 // So requests arriving while a batch is counting are admitted, uploaded and
-// oriented on the device concurrently with it and join the next batch.  No
+// oriented on the device concurrently with it and join their lane's next
+// batch, and a small request never queues behind a large one: not for its
+// build (the small lane's own prep thread) and not for its count (the small
+// lane's own count stream).  On the device, the small lane's streams have the
+// higher priority, and the large lane's persistent count kernel runs with
+// reserve_blocks fewer blocks per SM than fit, so the block scheduler has
+// room for the small lane's kernels while a large batch is running.  No
 // kernel waits on another: the only waits are host-side and bounded (the
 // batch watchdog, batch_timeout_ms); a batch that does not finish fails its
 // requests with TC_E_TIMEOUT and stops the server from admitting more work.
@@ -36,8 +44,11 @@ using tc::set_error;
 
 enum ReqState { kQueued, kPreparing, kReady, kCounting, kDone, kFailed };
 
+constexpr int kSmall = 0, kLarge = 1, kLanes = 2;
+
 struct Request {
     uint64_t id = 0, key = 0;
+    int lane = kLarge;
     std::vector<int64_t> src, dst;
     int64_t n_nodes = 0;
     Clock::time_point t_submit;
@@ -55,24 +66,32 @@ struct Resident {
     size_t bytes = 0;
     uint64_t last_use = 0;
     int in_use = 0;
+    int lane = kLarge;  // the graph is bound to this lane's count context
 };
 
 }  // namespace
 
-struct tc_server {
+// One size class of requests: its queues, contexts and threads.
+struct Lane {
     tc_ctx *count_ctx = nullptr, *prep_ctx = nullptr;
+    cudaStream_t own_streams[2] = {nullptr, nullptr};  // prioritised streams (small lane), destroyed last
+    std::deque<Request *> queued, ready;
+    std::thread prep_thr, count_thr;
+};
+
+struct tc_server {
+    Lane lane[2];  // kSmall, kLarge
     tc_server_config cfg{};
+    int64_t small_edges = 0;  // requests with at most this many edges take the small lane (< 0: none)
     size_t budget = 0, used = 0;
     std::mutex mu;
     std::condition_variable cv;
-    std::deque<Request *> queued, ready;
     std::unordered_map<uint64_t, Request *> reqs;
     std::unordered_map<uint64_t, Resident> cache;
     uint64_t next_id = 1, tick = 0;
     bool stopping = false;
     int fault = TC_OK;  // set when a batch failed; no more admissions
     tc_server_stats stats{};
-    std::thread prep_thr, count_thr;
 };
 
 namespace {
@@ -106,14 +125,17 @@ bool make_room(tc_server *s, size_t need) {
     return true;
 }
 
-void prep_loop(tc_server *s) {
+int lane_of(const tc_server *s, int64_t edges) { return s->small_edges >= 0 && edges <= s->small_edges ? kSmall : kLarge; }
+
+void prep_loop(tc_server *s, int li) {
+    Lane &L = s->lane[li];
     std::unique_lock<std::mutex> lk(s->mu);
     for (;;) {
-        s->cv.wait(lk, [&] { return s->stopping || !s->queued.empty(); });
+        s->cv.wait(lk, [&] { return s->stopping || !L.queued.empty(); });
         if (s->stopping) return;
-        Request *r = s->queued.front();
+        Request *r = L.queued.front();
         if (s->fault != TC_OK) {
-            s->queued.pop_front();
+            L.queued.pop_front();
             finish(s, r, TC_E_STATE, "server stopped admitting after a failed batch");
             s->cv.notify_all();
             continue;
@@ -121,19 +143,19 @@ void prep_loop(tc_server *s) {
         if (r->key) {
             auto it = s->cache.find(r->key);
             if (it != s->cache.end()) {  // resident: no preprocessing
-                s->queued.pop_front();
+                L.queued.pop_front();
                 it->second.in_use++;
                 it->second.last_use = ++s->tick;
                 r->g = it->second.g;
                 r->state = kReady;
                 s->stats.cache_hits++;
-                s->ready.push_back(r);
+                s->lane[it->second.lane].ready.push_back(r);
                 s->cv.notify_all();
                 continue;
             }
         }
         if (r->src.empty() && r->dst.empty() && r->key) {
-            s->queued.pop_front();
+            L.queued.pop_front();
             finish(s, r, TC_E_STATE, "graph key is not resident and no edges were given");
             s->cv.notify_all();
             continue;
@@ -141,7 +163,7 @@ void prep_loop(tc_server *s) {
         const int64_t n = (int64_t)r->src.size();
         const size_t need = prep_bytes(n);
         if (need > s->budget) {
-            s->queued.pop_front();
+            L.queued.pop_front();
             finish(s, r, TC_E_NOMEM, "request needs more device memory than the whole budget");
             s->cv.notify_all();
             continue;
@@ -150,14 +172,14 @@ void prep_loop(tc_server *s) {
             s->cv.wait_for(lk, std::chrono::milliseconds(5));
             continue;
         }
-        s->queued.pop_front();
+        L.queued.pop_front();
         s->used += need;
         r->state = kPreparing;
         lk.unlock();
         tc_graph *g = nullptr;
-        int st = tc_graph_from_edges(s->prep_ctx, r->src.data(), r->dst.data(), n, r->n_nodes, s->cfg.tie, &g);
+        int st = tc_graph_from_edges(L.prep_ctx, r->src.data(), r->dst.data(), n, r->n_nodes, s->cfg.tie, &g);
         std::string err = st == TC_OK ? std::string() : std::string(tc_last_error());
-        if (st == TC_OK) st = tc::graph_rebind(g, s->count_ctx);
+        if (st == TC_OK) st = tc::graph_rebind(g, L.count_ctx);
         lk.lock();
         s->used -= need;
         std::vector<int64_t>().swap(r->src);
@@ -177,37 +199,43 @@ void prep_loop(tc_server *s) {
             res.bytes = bytes;
             res.in_use = 1;
             res.last_use = ++s->tick;
+            res.lane = li;
         } else {
             r->owns_graph = true;
         }
         r->state = kReady;
-        s->ready.push_back(r);
+        L.ready.push_back(r);
         s->cv.notify_all();
     }
 }
 
-void count_loop(tc_server *s) {
+void count_loop(tc_server *s, int li) {
+    Lane &L = s->lane[li];
     std::unique_lock<std::mutex> lk(s->mu);
     for (;;) {
-        s->cv.wait(lk, [&] { return s->stopping || !s->ready.empty(); });
-        if (s->stopping && s->ready.empty()) return;
+        s->cv.wait(lk, [&] { return s->stopping || !L.ready.empty(); });
+        if (s->stopping && L.ready.empty()) return;
         std::vector<Request *> batch;
-        while (!s->ready.empty() && (int)batch.size() < s->cfg.max_batch) {
-            batch.push_back(s->ready.front());
-            s->ready.pop_front();
+        while (!L.ready.empty() && (int)batch.size() < s->cfg.max_batch) {
+            batch.push_back(L.ready.front());
+            L.ready.pop_front();
             batch.back()->state = kCounting;
         }
+        // a batch is counted in the stats when it is taken (so a caller can
+        // see that one is in flight)
+        s->stats.batches++;
+        if (li == kSmall) s->stats.small_batches++;
+        else s->stats.large_batches++;
+        s->stats.max_batch_seen = std::max<int64_t>(s->stats.max_batch_seen, (int64_t)batch.size());
         lk.unlock();
         std::vector<tc_graph *> gs(batch.size());
         for (size_t i = 0; i < batch.size(); ++i) gs[i] = batch[i]->g;
         std::vector<uint64_t> outs(batch.size());
         float kms = 0;
-        int st = tc::count_graphs_direct(s->count_ctx, gs.data(), (int)gs.size(), outs.data(),
+        int st = tc::count_graphs_direct(L.count_ctx, gs.data(), (int)gs.size(), outs.data(),
                                          s->cfg.batch_timeout_ms, &kms);
         std::string err = st == TC_OK ? std::string() : std::string(tc_last_error());
         lk.lock();
-        s->stats.batches++;
-        s->stats.max_batch_seen = std::max<int64_t>(s->stats.max_batch_seen, (int64_t)batch.size());
         if (st == TC_E_TIMEOUT) s->fault = st;
         for (size_t i = 0; i < batch.size(); ++i) {
             Request *r = batch[i];
@@ -264,28 +292,63 @@ int tc_server_create(tc_ctx *ctx, const tc_server_config *cfg, tc_server **out) 
     if (s->cfg.max_batch <= 0) s->cfg.max_batch = 256;
     if (s->cfg.batch_timeout_ms <= 0) s->cfg.batch_timeout_ms = 60000;
     if (s->cfg.tie != TC_TIE_ID_ASC) s->cfg.tie = TC_TIE_REFERENCE;
-    int dev = ctx->device;
-    int st = tc_ctx_create(dev, &s->count_ctx);
-    if (st == TC_OK) st = tc_ctx_create(dev, &s->prep_ctx);
-    if (st == TC_OK) {
-        tc_tuning t;
-        tc_ctx_get_tuning(ctx, &t);
-        t.blocks_per_sm = -1;
-        st = tc_ctx_set_tuning(s->count_ctx, &t);
+    s->small_edges = s->cfg.small_edges == 0 ? ((int64_t)1 << 20) : s->cfg.small_edges;
+    const int reserve = s->cfg.reserve_blocks == 0 ? 1 : std::max(0, (int)s->cfg.reserve_blocks);
+    const int dev = ctx->device;
+    int st = cudaSetDevice(dev) == cudaSuccess ? TC_OK : set_error(TC_E_CUDA, "cudaSetDevice(%d) failed", dev);
+    int prio_lo = 0, prio_hi = 0;
+    if (st == TC_OK && cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) != cudaSuccess)
+        st = set_error(TC_E_CUDA, "stream priority query failed");
+    tc_tuning base;
+    if (st == TC_OK) st = tc_ctx_get_tuning(ctx, &base);
+    for (int li = 0; li < kLanes && st == TC_OK; ++li) {
+        Lane &L = s->lane[li];
+        st = tc_ctx_create(dev, &L.count_ctx);
+        if (st == TC_OK) st = tc_ctx_create(dev, &L.prep_ctx);
+        if (st == TC_OK && li == kSmall) {
+            // the small lane's streams at the highest priority: its blocks are
+            // scheduled first whenever a large batch frees an SM slot
+            for (int q = 0; q < 2 && st == TC_OK; ++q)
+                if (cudaStreamCreateWithPriority(&L.own_streams[q], cudaStreamNonBlocking, prio_hi) != cudaSuccess)
+                    st = set_error(TC_E_CUDA, "prioritised stream creation failed");
+            if (st == TC_OK) st = tc_ctx_set_stream(L.count_ctx, L.own_streams[0]);
+            if (st == TC_OK) st = tc_ctx_set_stream(L.prep_ctx, L.own_streams[1]);
+        }
+        if (st == TC_OK) {
+            tc_tuning t = base;
+            t.blocks_per_sm = -1;
+            st = tc_ctx_set_tuning(L.count_ctx, &t);
+            if (st == TC_OK && li == kLarge && reserve > 0 && s->small_edges >= 0) {
+                // leave `reserve` block slots per SM to the small lane
+                tc_tuning now;
+                st = tc_ctx_get_tuning(L.count_ctx, &now);
+                if (st == TC_OK && now.blocks_per_sm > reserve) {
+                    t.blocks_per_sm = now.blocks_per_sm - reserve;
+                    st = tc_ctx_set_tuning(L.count_ctx, &t);
+                }
+            }
+        }
     }
     size_t total = 0;
     if (st == TC_OK) st = tc_ctx_device_info(ctx, nullptr, nullptr, &total);
     if (st != TC_OK) {
-        tc_ctx_destroy(s->count_ctx);
-        tc_ctx_destroy(s->prep_ctx);
+        const std::string why = tc_last_error();
+        for (Lane &L : s->lane) {
+            tc_ctx_destroy(L.count_ctx);
+            tc_ctx_destroy(L.prep_ctx);
+            for (cudaStream_t q : L.own_streams)
+                if (q) cudaStreamDestroy(q);
+        }
         delete s;
-        return st;
+        return set_error(st, "server creation failed: %s", why.c_str());
     }
     const double frac = s->cfg.hbm_budget_frac > 0 ? s->cfg.hbm_budget_frac : 0.8;
     s->budget = s->cfg.hbm_budget_bytes > 0 ? (size_t)s->cfg.hbm_budget_bytes : (size_t)(frac * (double)total);
     s->stats.budget_bytes = (int64_t)s->budget;
-    s->prep_thr = std::thread(prep_loop, s);
-    s->count_thr = std::thread(count_loop, s);
+    for (int li = 0; li < kLanes; ++li) {
+        s->lane[li].prep_thr = std::thread(prep_loop, s, li);
+        s->lane[li].count_thr = std::thread(count_loop, s, li);
+    }
     *out = s;
     return TC_OK;
 }
@@ -298,9 +361,10 @@ int tc_server_submit(tc_server *s, uint64_t graph_key, const int64_t *src, const
     r->key = graph_key;
     r->n_nodes = n_nodes;
     r->t_submit = Clock::now();
+    r->lane = lane_of(s, n_edges);
     {
-        // resident key: pin the graph and go straight to the count thread,
-        // without copying the edges
+        // resident key: pin the graph and go straight to the count thread of
+        // the lane that holds it, without copying the edges
         std::lock_guard<std::mutex> lk(s->mu);
         if (s->stopping) {
             delete r;
@@ -311,10 +375,11 @@ int tc_server_submit(tc_server *s, uint64_t graph_key, const int64_t *src, const
             it->second.in_use++;
             it->second.last_use = ++s->tick;
             r->g = it->second.g;
+            r->lane = it->second.lane;
             r->state = kReady;
             r->id = s->next_id++;
             s->reqs[r->id] = r;
-            s->ready.push_back(r);
+            s->lane[r->lane].ready.push_back(r);
             s->stats.submitted++;
             s->stats.cache_hits++;
             *request_id = r->id;
@@ -333,7 +398,7 @@ int tc_server_submit(tc_server *s, uint64_t graph_key, const int64_t *src, const
     }
     r->id = s->next_id++;
     s->reqs[r->id] = r;
-    s->queued.push_back(r);
+    s->lane[r->lane].queued.push_back(r);
     s->stats.submitted++;
     *request_id = r->id;
     s->cv.notify_all();
@@ -370,7 +435,7 @@ int tc_server_get_stats(tc_server *s, tc_server_stats *out) {
     *out = s->stats;
     out->resident_graphs = (int64_t)s->cache.size();
     out->used_bytes = (int64_t)s->used;
-    out->queued = (int64_t)s->queued.size();
+    out->queued = (int64_t)(s->lane[kSmall].queued.size() + s->lane[kLarge].queued.size());
     return TC_OK;
 }
 
@@ -379,13 +444,15 @@ int tc_server_destroy(tc_server *s) {
     {
         std::unique_lock<std::mutex> lk(s->mu);
         // drain: let admitted and ready work finish, fail what is still queued
-        while (!s->queued.empty()) {
-            Request *r = s->queued.front();
-            s->queued.pop_front();
-            finish(s, r, TC_E_STATE, "server shut down before the request was admitted");
-        }
+        for (Lane &L : s->lane)
+            while (!L.queued.empty()) {
+                Request *r = L.queued.front();
+                L.queued.pop_front();
+                finish(s, r, TC_E_STATE, "server shut down before the request was admitted");
+            }
         s->cv.wait_for(lk, std::chrono::milliseconds(s->cfg.batch_timeout_ms), [&] {
-            if (!s->ready.empty()) return false;
+            for (Lane &L : s->lane)
+                if (!L.ready.empty()) return false;
             for (auto &kv : s->reqs)
                 if (kv.second->state == kPreparing || kv.second->state == kCounting) return false;
             return true;
@@ -393,13 +460,18 @@ int tc_server_destroy(tc_server *s) {
         s->stopping = true;
         s->cv.notify_all();
     }
-    s->prep_thr.join();
-    s->count_thr.join();
-    // A batch that overran its watchdog may still be running on the count
+    for (Lane &L : s->lane) {
+        L.prep_thr.join();
+        L.count_thr.join();
+    }
+    // A batch that overran its watchdog may still be running on a count
     // stream: its graphs must not be freed under it.  Wait for it (bounded);
     // if it is still running, leave the device memory allocated.
-    const bool drained = s->fault == TC_OK ||
-                         stream_drained(s->count_ctx->stream, std::max<int64_t>(s->cfg.batch_timeout_ms, 5000));
+    bool drained = true;
+    if (s->fault != TC_OK)
+        for (Lane &L : s->lane)
+            drained = drained &&
+                      stream_drained(L.count_ctx->stream, std::max<int64_t>(s->cfg.batch_timeout_ms, 5000));
     for (auto &kv : s->reqs) {
         if (drained && kv.second->owns_graph && kv.second->g) tc_graph_destroy(kv.second->g);
         delete kv.second;
@@ -409,8 +481,17 @@ int tc_server_destroy(tc_server *s) {
         return set_error(TC_E_TIMEOUT, "a timed-out batch is still running; its device memory was left allocated");
     }
     for (auto &kv : s->cache) tc_graph_destroy(kv.second.g);
-    tc_ctx_destroy(s->count_ctx);
-    tc_ctx_destroy(s->prep_ctx);
+    for (Lane &L : s->lane) {
+        // a context's stream is synchronised when its last object goes
+        tc_ctx_destroy(L.count_ctx);
+        tc_ctx_destroy(L.prep_ctx);
+    }
+    for (Lane &L : s->lane)
+        for (cudaStream_t q : L.own_streams)
+            if (q) {
+                cudaStreamSynchronize(q);
+                cudaStreamDestroy(q);
+            }
     delete s;
     return TC_OK;
 }
