@@ -321,6 +321,8 @@ typedef struct tc_server_config {
     int32_t reserve_blocks;   /* count-kernel block slots per SM the large lane leaves free (0: 1; < 0: none) */
     int64_t small_edges;      /* requests with at most this many edges take the small lane (0: 2^20; < 0: one
                                  lane for all) */
+    int64_t staging_bytes;    /* page-locked host area that submitted edge lists are copied into, so builds
+                                 upload them at the link's rate (0: 1 GiB; < 0: none, pageable copies) */
 } tc_server_config;
 
 typedef struct tc_server_stats {
@@ -333,7 +335,8 @@ typedef struct tc_server_stats {
 TC_API int tc_server_create(tc_ctx *ctx, const tc_server_config *cfg, tc_server **out);
 /* Queue a count.  graph_key != 0 keeps the oriented graph resident under that
  * key; a later request with the same key is counted without preprocessing (it
- * may then pass no edges).  The edge arrays are copied before returning. */
+ * may then pass no edges).  The edge arrays are copied before returning (into
+ * the pinned staging area when it has room). */
 TC_API int tc_server_submit(tc_server *s, uint64_t graph_key, const int64_t *src, const int64_t *dst, int64_t n_edges,
                             int64_t n_nodes, uint64_t *request_id);
 /* TC_OK with the count and the latency (submit -> result) once done; the

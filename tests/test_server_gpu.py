@@ -135,3 +135,16 @@ def test_one_lane_when_small_edges_is_negative(ctx):
         got = [srv.wait(srv.submit(s, d))[0] for s, d in gs]
         st = srv.stats()
     assert got == alone and st["small_batches"] == 0 and st["large_batches"] >= 1
+
+
+@pytest.mark.parametrize("staging", [-1, 4 << 20])
+def test_staging_area_full_or_absent(ctx, staging):
+    """Edge lists that do not fit the pinned staging area (a 4 MiB area, or
+    none) are kept in pageable memory; results are the same either way, and
+    the area's ranges are reused once builds release them."""
+    gs = _graphs()
+    alone = [ctx.count(ctx.graph_from_edges(s, d)) for s, d in gs]
+    with tc.Server(ctx, staging_bytes=staging) as srv:
+        for _ in range(2):
+            ids = [srv.submit(s, d) for s, d in gs]
+            assert [srv.wait(i)[0] for i in ids] == alone

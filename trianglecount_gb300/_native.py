@@ -44,7 +44,7 @@ class CountStats(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_frac", C.c_double), ("hbm_budget_bytes", C.c_int64), ("max_batch", C.c_int32),
                 ("tie", C.c_int32), ("batch_timeout_ms", C.c_int32), ("reserve_blocks", C.c_int32),
-                ("small_edges", C.c_int64)]
+                ("small_edges", C.c_int64), ("staging_bytes", C.c_int64)]
 
 
 class ServerStats(C.Structure):

@@ -167,12 +167,14 @@ class Server:
 
     def __init__(self, ctx: "Context", hbm_budget_frac: float = 0.8, hbm_budget_bytes: int = 0,
                  max_batch: int = 256, tie="reference", batch_timeout_ms: int = 60000, reserve_blocks: int = 0,
-                 small_edges: int = 0):
+                 small_edges: int = 0, staging_bytes: int = 0):
         """small_edges: requests with at most this many edges take the small
         lane (0: 2^20, < 0: one lane); reserve_blocks: count-kernel block slots
-        per SM the large lane leaves to the small one (0: 1, < 0: none)."""
+        per SM the large lane leaves to the small one (0: 1, < 0: none);
+        staging_bytes: pinned host area for submitted edge lists (0: 1 GiB,
+        < 0: none)."""
         cfg = N.ServerConfig(hbm_budget_frac, hbm_budget_bytes, max_batch, _tie(tie), batch_timeout_ms,
-                             reserve_blocks, small_edges)
+                             reserve_blocks, small_edges, staging_bytes)
         h = C.c_void_p()
         N.call("tc_server_create", ctx.handle, C.byref(cfg), C.byref(h))
         self._h = h

@@ -319,10 +319,10 @@ __device__ __forceinline__ uint32_t sorted_probe(const int *a, int n, int x) {
 
 // Membership of x >= 0 in the table, by the table's mode (kPairsOnly: the
 // kernel instance that builds pair tables only).
-template <bool kPairsOnly>
+template <bool kPairsOnly, bool kSortedOk = false>
 __device__ __forceinline__ uint32_t probe_any(const int *tab, uint32_t mask, int shift, int x, int mode) {
     if (kPairsOnly) return pair_probe(tab, mask >> 1, shift, x);
-    if (mode == kSorted) return sorted_probe(tab, (int)mask, x);  // mask = the list's length
+    if (kSortedOk && mode == kSorted) return sorted_probe(tab, (int)mask, x);  // mask = the list's length
     return mode == kCuckoo ? cuckoo_probe(tab, shift, x) : table_probe(tab, mask, shift, x);
 }
 
@@ -414,7 +414,7 @@ struct Task {
 // out-neighbours v of x, skipped unless d+(v) <= d+(x); the others are
 // in-neighbours u.  Returns this lane's hit count; with per_root set, hits are
 // also credited to their root (x for out-partners, u for in-partners).
-template <bool kPerRoot, bool kBitmap = false, bool kPairsOnly = false>
+template <bool kPerRoot, bool kBitmap = false, bool kPairsOnly = false, bool kSortedOk = false>
 __device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
                                                    const Task &T, int j0, int j1, const int *tab, uint32_t mask,
                                                    int shift, int mode, int long_list, int lane,
@@ -472,7 +472,7 @@ __device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ r
             } else if (mode == kCuckoo) {
 #pragma unroll
                 for (int i = 0; i < 4; ++i) h += (uint32_t)(x[i] >= 0) & cuckoo_probe(tab, shift, x[i]);
-            } else if (mode == kSorted) {  // four independent searches in flight
+            } else if (kSortedOk && mode == kSorted) {  // four independent searches in flight
 #pragma unroll
                 for (int i = 0; i < 4; ++i) h += (uint32_t)(x[i] >= 0) & sorted_probe(tab, (int)mask, x[i]);
             } else {
@@ -512,7 +512,8 @@ __device__ __forceinline__ uint32_t probe_partners(const int32_t *__restrict__ r
         const int own = kPerRoot ? __shfl_sync(kFull, owner, seg) : 0;
         if (t < total) {
             const int y = __ldg(col + s_seg + (t - ex_seg));
-            const uint32_t h = kBitmap ? bitmap_probe(tab, y) : probe_any<kPairsOnly>(tab, mask, shift, y, mode);
+            const uint32_t h =
+                kBitmap ? bitmap_probe(tab, y) : probe_any<kPairsOnly, kSortedOk>(tab, mask, shift, y, mode);
             hits += h;
             if (kPerRoot && h) atomicAdd(per_root + own, 1ull);
         }
@@ -1244,11 +1245,17 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
         const int per = (n_part + ns - 1) / ns;
         const int j0 = si * per, j1 = min(n_part, j0 + per);
         const uint32_t pmask = cached_mode == kSorted ? (uint32_t)tl : mask;
-        // partners per grab: kHeavyChunk, or fewer when the unit has fewer than
-        // kHeavyChunk partners per warp, so that every warp gets a grab (a hub's
-        // unit in a halo part holds only that part's in-partners: at 16 per
-        // grab most warps would wait at the barrier below)
-        const int chunk = max(1, min(kHeavyChunk, (j1 - j0 + kWarpsPerBlock - 1) / kWarpsPerBlock));
+        // partners per grab: kHeavyChunk; in a halo part (roots a prefix of the
+        // rows) fewer when the unit has fewer than kHeavyChunk partners per
+        // warp, so that every warp gets a grab.  A hub's unit in a halo part
+        // holds only that part's in-partners: at 16 per grab several warps
+        // waited at the barrier below (barrier stalls 5.4 per issue on R-MAT
+        // 21's eight parts; R-MAT 23's eight parts 41.0 -> 39.1 ms).  Whole
+        // graphs keep 16: smaller grabs there cost 2-3% (fewer short lists per
+        // grab to flatten across the lanes).
+        const int chunk = G.n_roots < G.n_rows
+                              ? max(1, min(kHeavyChunk, (j1 - j0 + kWarpsPerBlock - 1) / kWarpsPerBlock))
+                              : kHeavyChunk;
         uint32_t hits = 0;
         for (;;) {
             int c = 0;
@@ -1256,7 +1263,7 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
             c = __shfl_sync(kFull, c, 0);
             const int jb = j0 + c * chunk;
             if (jb >= j1) break;
-            hits += probe_partners<kPerRoot, false, kPairsOnly>(rp, col, T, jb, min(jb + chunk, j1), cached_tab,
+            hits += probe_partners<kPerRoot, false, kPairsOnly, kStage>(rp, col, T, jb, min(jb + chunk, j1), cached_tab,
                                                                 pmask, shift, cached_mode, P.long_list, lane,
                                                                 G.per_root);
         }
@@ -1358,7 +1365,7 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
             __syncwarp();
             uint32_t hits = 0;
             for (int jb = 0; jb < n_part; jb += kWarp)
-                hits += probe_partners<kPerRoot, false, kPairsOnly>(rp, col, T, jb, min(jb + kWarp, n_part), tab, mask,
+                hits += probe_partners<kPerRoot, false, kPairsOnly, kStage>(rp, col, T, jb, min(jb + kWarp, n_part), tab, mask,
                                                                     shift, mode, P.long_list, lane, G.per_root);
             __syncwarp();
             if (!kPerRoot) acc += hits;

@@ -25,11 +25,14 @@
 // kernel waits on another: the only waits are host-side and bounded (the
 // batch watchdog, batch_timeout_ms); a batch that does not finish fails its
 // requests with TC_E_TIMEOUT and stops the server from admitting more work.
+// Submitted edge lists are copied (on up to 8 threads) into a pinned host
+// staging area when it has room, so the build uploads them at the link's rate.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <mutex>
 #include <thread>
 #include <unordered_map>
@@ -49,7 +52,10 @@ constexpr int kSmall = 0, kLarge = 1, kLanes = 2;
 struct Request {
     uint64_t id = 0, key = 0;
     int lane = kLarge;
-    std::vector<int64_t> src, dst;
+    std::vector<int64_t> src, dst;  // the edges, when they did not fit the pinned staging area
+    int64_t *h_src = nullptr, *h_dst = nullptr;  // the edges in the pinned staging area
+    size_t stage_off = 0, stage_len = 0;         // their byte range there (stage_len 0: not staged)
+    int64_t n_edges = 0;
     int64_t n_nodes = 0;
     Clock::time_point t_submit;
     double latency_ms = 0;
@@ -79,8 +85,52 @@ struct Lane {
     std::thread prep_thr, count_thr;
 };
 
+// First-fit allocator over one pinned host area (byte ranges), so that
+// submitted edge lists are uploaded from page-locked memory at the link's
+// rate instead of being staged through the driver.  Caller holds the mutex.
+struct PinnedArena {
+    unsigned char *base = nullptr;
+    size_t size = 0;
+    std::map<size_t, size_t> free_;  // offset -> length, coalesced
+    void init(unsigned char *b, size_t n) {
+        base = b;
+        size = n;
+        free_.clear();
+        if (n) free_[0] = n;
+    }
+    bool take(size_t n, size_t *off) {
+        n = (n + 255) & ~(size_t)255;
+        for (auto it = free_.begin(); it != free_.end(); ++it)
+            if (it->second >= n) {
+                *off = it->first;
+                const size_t rest = it->second - n, at = it->first + n;
+                free_.erase(it);
+                if (rest) free_[at] = rest;
+                return true;
+            }
+        return false;
+    }
+    void give(size_t off, size_t n) {
+        n = (n + 255) & ~(size_t)255;
+        auto it = free_.emplace(off, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+};
+
 struct tc_server {
     Lane lane[2];  // kSmall, kLarge
+    PinnedArena arena;
     tc_server_config cfg{};
     int64_t small_edges = 0;  // requests with at most this many edges take the small lane (< 0: none)
     size_t budget = 0, used = 0;
@@ -100,7 +150,10 @@ namespace {
 // buffers of 2n, flags, positions and the CSR arrays.
 size_t prep_bytes(int64_t n) { return (size_t)n * 16 * 2 + (size_t)n * 2 * (1 + 4 + 8) + ((size_t)1 << 20); }
 
+void release_edges(tc_server *s, Request *r);
+
 void finish(tc_server *s, Request *r, int status, const char *err) {
+    release_edges(s, r);
     r->status = status;
     r->state = status == TC_OK ? kDone : kFailed;
     if (err) r->error = err;
@@ -125,6 +178,33 @@ bool make_room(tc_server *s, size_t need) {
     return true;
 }
 
+// memcpy of n bytes on up to 8 threads (a large edge list is copied at the
+// host's memory bandwidth rather than one core's).
+void copy_parallel(void *dst, const void *src, size_t n) {
+    const size_t kPer = (size_t)32 << 20;
+    const int T = (int)std::min<size_t>(8, (n + kPer - 1) / kPer);
+    if (T <= 1) {
+        memcpy(dst, src, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    const size_t step = (n + T - 1) / T;
+    for (int t = 0; t < T; ++t) {
+        const size_t a = std::min(n, (size_t)t * step), b = std::min(n, a + step);
+        th.emplace_back([=] { memcpy((unsigned char *)dst + a, (const unsigned char *)src + a, b - a); });
+    }
+    for (auto &x : th) x.join();
+}
+
+// Drops a request's edge lists (staging range or vectors).  Caller holds mu.
+void release_edges(tc_server *s, Request *r) {
+    if (r->stage_len) s->arena.give(r->stage_off, r->stage_len);
+    r->stage_len = 0;
+    r->h_src = r->h_dst = nullptr;
+    std::vector<int64_t>().swap(r->src);
+    std::vector<int64_t>().swap(r->dst);
+}
+
 int lane_of(const tc_server *s, int64_t edges) { return s->small_edges >= 0 && edges <= s->small_edges ? kSmall : kLarge; }
 
 void prep_loop(tc_server *s, int li) {
@@ -144,6 +224,7 @@ void prep_loop(tc_server *s, int li) {
             auto it = s->cache.find(r->key);
             if (it != s->cache.end()) {  // resident: no preprocessing
                 L.queued.pop_front();
+                release_edges(s, r);
                 it->second.in_use++;
                 it->second.last_use = ++s->tick;
                 r->g = it->second.g;
@@ -154,13 +235,13 @@ void prep_loop(tc_server *s, int li) {
                 continue;
             }
         }
-        if (r->src.empty() && r->dst.empty() && r->key) {
+        if (r->n_edges == 0 && r->key) {
             L.queued.pop_front();
             finish(s, r, TC_E_STATE, "graph key is not resident and no edges were given");
             s->cv.notify_all();
             continue;
         }
-        const int64_t n = (int64_t)r->src.size();
+        const int64_t n = r->n_edges;
         const size_t need = prep_bytes(n);
         if (need > s->budget) {
             L.queued.pop_front();
@@ -177,13 +258,14 @@ void prep_loop(tc_server *s, int li) {
         r->state = kPreparing;
         lk.unlock();
         tc_graph *g = nullptr;
-        int st = tc_graph_from_edges(L.prep_ctx, r->src.data(), r->dst.data(), n, r->n_nodes, s->cfg.tie, &g);
+        const int64_t *es = r->stage_len ? r->h_src : r->src.data();
+        const int64_t *ed = r->stage_len ? r->h_dst : r->dst.data();
+        int st = tc_graph_from_edges(L.prep_ctx, es, ed, n, r->n_nodes, s->cfg.tie, &g);
         std::string err = st == TC_OK ? std::string() : std::string(tc_last_error());
         if (st == TC_OK) st = tc::graph_rebind(g, L.count_ctx);
         lk.lock();
         s->used -= need;
-        std::vector<int64_t>().swap(r->src);
-        std::vector<int64_t>().swap(r->dst);
+        release_edges(s, r);  // the build has read them (its upload finished before it returned)
         if (st != TC_OK) {
             if (g) tc_graph_destroy(g);
             finish(s, r, st, err.c_str());
@@ -342,6 +424,12 @@ int tc_server_create(tc_ctx *ctx, const tc_server_config *cfg, tc_server **out) 
         delete s;
         return set_error(st, "server creation failed: %s", why.c_str());
     }
+    const int64_t stage = s->cfg.staging_bytes == 0 ? ((int64_t)1 << 30) : s->cfg.staging_bytes;
+    if (stage > 0) {
+        void *h = nullptr;
+        if (cudaMallocHost(&h, (size_t)stage) == cudaSuccess) s->arena.init((unsigned char *)h, (size_t)stage);
+        else cudaGetLastError();  // no staging area: edges are kept in pageable memory
+    }
     const double frac = s->cfg.hbm_budget_frac > 0 ? s->cfg.hbm_budget_frac : 0.8;
     s->budget = s->cfg.hbm_budget_bytes > 0 ? (size_t)s->cfg.hbm_budget_bytes : (size_t)(frac * (double)total);
     s->stats.budget_bytes = (int64_t)s->budget;
@@ -387,12 +475,31 @@ int tc_server_submit(tc_server *s, uint64_t graph_key, const int64_t *src, const
             return TC_OK;
         }
     }
+    r->n_edges = n_edges;
     if (n_edges > 0) {
-        r->src.assign(src, src + n_edges);
-        r->dst.assign(dst, dst + n_edges);
+        // into the pinned staging area when it has room, else into vectors
+        const size_t half = ((size_t)n_edges * sizeof(int64_t) + 255) & ~(size_t)255;
+        size_t off = 0;
+        bool staged;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            staged = s->arena.size && s->arena.take(2 * half, &off);
+        }
+        if (staged) {
+            r->stage_off = off;
+            r->stage_len = 2 * half;
+            r->h_src = (int64_t *)(s->arena.base + off);
+            r->h_dst = (int64_t *)(s->arena.base + off + half);
+            copy_parallel(r->h_src, src, (size_t)n_edges * sizeof(int64_t));
+            copy_parallel(r->h_dst, dst, (size_t)n_edges * sizeof(int64_t));
+        } else {
+            r->src.assign(src, src + n_edges);
+            r->dst.assign(dst, dst + n_edges);
+        }
     }
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stopping) {
+        release_edges(s, r);
         delete r;
         return set_error(TC_E_STATE, "server is shutting down");
     }
@@ -477,6 +584,7 @@ int tc_server_destroy(tc_server *s) {
         delete kv.second;
     }
     if (!drained) {
+        if (s->arena.base) cudaFreeHost(s->arena.base);  // the builds that read it have returned
         delete s;
         return set_error(TC_E_TIMEOUT, "a timed-out batch is still running; its device memory was left allocated");
     }
@@ -492,6 +600,7 @@ int tc_server_destroy(tc_server *s) {
                 cudaStreamSynchronize(q);
                 cudaStreamDestroy(q);
             }
+    if (s->arena.base) cudaFreeHost(s->arena.base);
     delete s;
     return TC_OK;
 }
