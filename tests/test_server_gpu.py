@@ -91,14 +91,16 @@ def test_batch_watchdog_reports_timeout(ctx):
 
 
 def test_small_requests_overtake_a_large_one_in_flight(ctx):
-    """An R-MAT 22 request (67 M edges, the large lane) is submitted first;
-    once its batch has been taken for counting, small requests (the small
-    lane) arrive.  They are built and counted beside the large batch on their
-    own streams and complete before it; every result equals its solo count."""
-    big = gen.rmat(22)
-    smalls = [gen.rmat(10, seed=300 + i) for i in range(3)] + [gen.chung_lu(5000, 8.0, seed=9)]
-    want_big = oracle.pipeline(*big)[2]
+    """An R-MAT 23 request (134 M edges, the large lane; its count alone takes
+    ~35 ms) is submitted first; once its batch has been taken for counting,
+    three small requests (the small lane) arrive.  They are built and counted
+    beside the large batch on their own streams and complete before it; every
+    result equals its solo count (the plain per-graph count)."""
+    big = gen.rmat(23)
+    smalls = [gen.rmat(9, seed=300 + i) for i in range(2)] + [gen.chung_lu(3000, 8.0, seed=9)]
+    want_big = ctx.count(ctx.graph_from_edges(*big))
     want_small = [ctx.count(ctx.graph_from_edges(s, d)) for s, d in smalls]
+    assert want_small[0] == oracle.pipeline(*smalls[0])[2]
     with tc.Server(ctx, max_batch=64) as srv:
         # warm both lanes (first-use set-up stays out of the race below)
         srv.wait(srv.submit(*smalls[0]))

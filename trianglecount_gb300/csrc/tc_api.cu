@@ -181,7 +181,7 @@ void capture_count(tc_graph *g, unsigned long long *res) {
     }
     int nl = 0;
     const int st = launch_count(g->d_desc, 1, (g->n_rows + 31) / 32, g->n_rows + 1, g->n_rows, g->sc, g->d_work, res,
-                                false, ctx->tuned, s, &nl, ctx->kev);
+                                false, ctx->tuned, s, &nl, ctx->kev, g->n_roots < g->n_rows);
     cudaGraph_t graph = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(s, &graph);
     cudaGraphExec_t exec = nullptr;
@@ -268,7 +268,7 @@ int enqueue_graph_count(tc_graph *g, unsigned long long *per_root, unsigned long
         return TC_OK;
     }
     return launch_count(g->d_desc, 1, chunks, g->n_rows + 1, g->n_rows, g->sc, g->d_work, res, per_root != nullptr,
-                        ctx->tuned, ctx->stream, launches, ctx->kev);
+                        ctx->tuned, ctx->stream, launches, ctx->kev, g->n_roots < g->n_rows);
 }
 
 int new_graph(tc_ctx *ctx, int64_t n_rows, int64_t nnz, int64_t n_roots, tc_graph **out) {
@@ -396,9 +396,11 @@ int count_graphs_direct(tc_ctx *ctx, tc_graph *const *graphs, int n, uint64_t *o
     cudaStream_t s = ctx->stream;
     std::vector<GraphDesc> desc((size_t)n);
     int64_t chunks = 0, cap = 0, vtot = 0, etot = 0, max_rows = 0;
+    bool halo_parts = false;
     for (int i = 0; i < n; ++i) {
         const tc_graph *g = graphs[i];
         if (g) max_rows = std::max(max_rows, g->n_rows);
+        if (g) halo_parts = halo_parts || g->n_roots < g->n_rows;
         if (!g || g->ctx->device != ctx->device) return set_error(TC_E_INVALID, "graph %d is null or on another device", i);
         memset(&desc[(size_t)i], 0, sizeof(GraphDesc));
         desc[(size_t)i].rp = g->rp;
@@ -434,7 +436,8 @@ int count_graphs_direct(tc_ctx *ctx, tc_graph *const *graphs, int n, uint64_t *o
     if (st == TC_OK && cudaEventRecord(ctx->ev[0], s) != cudaSuccess) st = set_error(TC_E_CUDA, "event record failed");
     if (st == TC_OK)
         st = launch_count(d_desc.p, n, chunks, vtot, max_rows, sc, (CountWork *)d_work.p,
-                          (unsigned long long *)(d_work.p + sizeof(CountWork)), false, ctx->tuned, s, nullptr);
+                          (unsigned long long *)(d_work.p + sizeof(CountWork)), false, ctx->tuned, s, nullptr, nullptr,
+                          halo_parts);
     if (st == TC_OK && cudaEventRecord(ctx->ev[1], s) != cudaSuccess) st = set_error(TC_E_CUDA, "event record failed");
     if (st == TC_OK && cudaMemcpyAsync(h_out, d_work.p, out_bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         st = set_error(TC_E_CUDA, "result read-back failed");
@@ -904,9 +907,11 @@ int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out)
     cudaStream_t s = ctx->stream;
     std::vector<GraphDesc> desc((size_t)n);
     int64_t chunks = 0, cap = 0, vtot = 0, etot = 0, max_rows = 0;
+    bool halo_parts = false;
     for (int i = 0; i < n; ++i) {
         tc_graph *g = graphs[i];
         if (g) max_rows = std::max(max_rows, g->n_rows);
+        if (g) halo_parts = halo_parts || g->n_roots < g->n_rows;
         if (!g || g->ctx != ctx) {
             tc_batch_destroy(b);
             return set_error(TC_E_INVALID, "graph %d is null or belongs to another context", i);
@@ -944,7 +949,8 @@ int tc_batch_create(tc_ctx *ctx, tc_graph *const *graphs, int n, tc_batch **out)
         st = set_error(TC_E_CUDA, "stream capture could not start");
     if (st == TC_OK) {
         int ls = launch_count(b->d_desc, n, chunks, vtot, max_rows, b->sc, b->d_work,
-                              (unsigned long long *)(b->d_work + 1), false, ctx->tuned, s, &b->launches, b->kev);
+                              (unsigned long long *)(b->d_work + 1), false, ctx->tuned, s, &b->launches, b->kev,
+                              halo_parts);
         cudaError_t e = cudaStreamEndCapture(s, &b->graph);
         if (ls != TC_OK) st = ls;
         else if (e != cudaSuccess) st = cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);

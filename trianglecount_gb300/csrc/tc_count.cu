@@ -1106,7 +1106,12 @@ __global__ void __launch_bounds__(kBigThreads, 1) heavy_bitmap_kernel(KParams P,
     }
 }
 
-template <bool kPerRoot, bool kPairsOnly, bool kStage = false>
+// kParts: the launch holds halo parts (roots a prefix of the rows): heavy
+// units grab fewer partners when they have few, and warp 0 takes the next
+// unit while the other warps finish the current one (below).  Whole graphs
+// get the instance without either: the same rules cost them 2-3 % (R-MAT 21
+// 6.03 -> 6.21 ms, R-MAT 23 33.8 -> 34.6 ms) even where they never fire.
+template <bool kPerRoot, bool kPairsOnly, bool kStage = false, bool kParts = false>
 __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KParams P) {
     extern __shared__ __align__(16) int smem[];
     __shared__ unsigned s_unit;
@@ -1147,37 +1152,52 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
     int cached_entry = -1, cached_tile = -1;
     int cached_mode = kLinear;
     const int *cached_tab = smem;
-    for (; !P.heavy_done;) {
-        if (warp == 0) {
-            unsigned unit = 0;
-            if (lane == 0) unit = atomicAdd(&P.work->heavy_cursor, 1u);
-            unit = __shfl_sync(kFull, unit, 0);
-            int e = -1;
-            if (unit < n_units && n_entries > 0) {
-                // last entry with unit_base <= unit (entries ascend; entry 0 starts at unit 0):
-                // 32-ary search, one dependent load per round
-                int lo = 0, hi = (int)n_entries;
-                while (hi - lo > kWarp) {
-                    const int step = (hi - lo + kWarp - 1) / kWarp;
-                    const int idx = lo + lane * step;
-                    const bool le = idx < hi && (unsigned)P.heavy[idx].unit_base <= unit;
-                    const unsigned m = __ballot_sync(kFull, le);
-                    lo += (31 - __clz(m)) * step;
-                    hi = min(hi, lo + step);
-                }
-                const bool le = lo + lane < hi && (unsigned)P.heavy[lo + lane].unit_base <= unit;
-                e = lo + 31 - __clz(__ballot_sync(kFull, le));
-            }
-            if (lane == 0) {
-                s_unit = unit;
-                s_entry = e;
-                s_chunk = 0;
-            }
+    // Warp 0 takes a unit: its number and heavy entry (-1 when none is left).
+    // With kParts it takes the next unit as soon as it has no partners of the
+    // current one left to probe, so the grab's atomic and the dependent loads
+    // of its 32-ary search overlap the other warps' last probes instead of
+    // idling the whole block after the unit (a halo part's units are many and
+    // small); otherwise at the top of each unit.
+    auto grab_next = [&]() {
+        unsigned unit = 0;
+        if (lane == 0) unit = atomicAdd(&P.work->heavy_cursor, 1u);
+        unit = __shfl_sync(kFull, unit, 0);
+        unsigned ne = n_entries, nu = n_units;
+        if (kParts) {  // re-read here rather than kept live across the probes
+            const unsigned long long pk = __ldg(&P.work->heavy_packed);
+            ne = (unsigned)min((unsigned long long)(pk >> 32), (unsigned long long)P.heavy_cap);
+            nu = (unsigned)(pk & 0xffffffffull);
         }
-        __syncthreads();
+        int e = -1;
+        if (unit < nu && ne > 0) {
+            // last entry with unit_base <= unit (entries ascend; entry 0 starts at unit 0):
+            // 32-ary search, one dependent load per round
+            int lo = 0, hi = (int)ne;
+            while (hi - lo > kWarp) {
+                const int step = (hi - lo + kWarp - 1) / kWarp;
+                const int idx = lo + lane * step;
+                const bool le = idx < hi && (unsigned)P.heavy[idx].unit_base <= unit;
+                const unsigned m = __ballot_sync(kFull, le);
+                lo += (31 - __clz(m)) * step;
+                hi = min(hi, lo + step);
+            }
+            const bool le = lo + lane < hi && (unsigned)P.heavy[lo + lane].unit_base <= unit;
+            e = lo + 31 - __clz(__ballot_sync(kFull, le));
+        }
+        if (lane == 0) {
+            s_unit = unit;
+            s_entry = e;
+            if (!kParts) s_chunk = 0;
+        }
+    };
+    if (kParts && !P.heavy_done && warp == 0) grab_next();
+    for (; !P.heavy_done;) {
+        if (!kParts && warp == 0) grab_next();
+        __syncthreads();  // this unit's s_unit / s_entry are set (and the last unit's probes are done)
         const unsigned unit = s_unit;
         const int ei = s_entry;
         if (ei < 0) break;
+        if (kParts && threadIdx.x == 0) s_chunk = 0;
         const HeavyEntry e = P.heavy[ei];
         const GraphDesc &G = P.gd[e.g];
         const int32_t *__restrict__ rp = G.rp;
@@ -1245,17 +1265,16 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
         const int per = (n_part + ns - 1) / ns;
         const int j0 = si * per, j1 = min(n_part, j0 + per);
         const uint32_t pmask = cached_mode == kSorted ? (uint32_t)tl : mask;
-        // partners per grab: kHeavyChunk; in a halo part (roots a prefix of the
-        // rows) fewer when the unit has fewer than kHeavyChunk partners per
-        // warp, so that every warp gets a grab.  A hub's unit in a halo part
+        // partners per grab: kHeavyChunk; in halo parts (kParts) fewer when the
+        // unit has fewer than kHeavyChunk partners per warp, so that every warp
+        // gets a grab.  A hub's unit in a halo part
         // holds only that part's in-partners: at 16 per grab several warps
         // waited at the barrier below (barrier stalls 5.4 per issue on R-MAT
         // 21's eight parts; R-MAT 23's eight parts 41.0 -> 39.1 ms).  Whole
         // graphs keep 16: smaller grabs there cost 2-3% (fewer short lists per
         // grab to flatten across the lanes).
-        const int chunk = G.n_roots < G.n_rows
-                              ? max(1, min(kHeavyChunk, (j1 - j0 + kWarpsPerBlock - 1) / kWarpsPerBlock))
-                              : kHeavyChunk;
+        const int chunk = kParts ? max(1, min(kHeavyChunk, (j1 - j0 + kWarpsPerBlock - 1) / kWarpsPerBlock))
+                                 : kHeavyChunk;
         uint32_t hits = 0;
         for (;;) {
             int c = 0;
@@ -1271,7 +1290,11 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
             if (e.g != cur_g) flush(e.g);
             acc += hits;
         }
-        __syncthreads();
+        if (kParts) {
+            if (warp == 0) grab_next();  // while the other warps finish their grabs
+        } else {
+            __syncthreads();
+        }
     }
     warp_dirty = block_dirty;  // the warp regions lie in the block's region
 
@@ -1429,6 +1452,10 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     TC_CUDA(cudaFuncSetAttribute(count_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
     TC_CUDA(cudaFuncSetAttribute(count_kernel<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)r.smem));
+    TC_CUDA(cudaFuncSetAttribute(count_kernel<false, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)r.smem));
+    TC_CUDA(cudaFuncSetAttribute(count_kernel<true, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)r.smem));
     TC_CUDA(cudaFuncSetAttribute(count_kernel<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)r.smem));
     int occ = 0;
@@ -1467,7 +1494,7 @@ static int record_kernel_event(cudaEvent_t ev, cudaStream_t s) {
 
 int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, int64_t total_vertices,
                  int64_t max_rows, const CountScratch &sc, CountWork *work, unsigned long long *results, bool per_root,
-                 const Tuned &tn, cudaStream_t s, int *launches, cudaEvent_t *kev) {
+                 const Tuned &tn, cudaStream_t s, int *launches, cudaEvent_t *kev, bool halo_parts) {
     KParams P;
     P.gd = d_desc;
     P.n_graphs = n_graphs;
@@ -1535,10 +1562,12 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
         if (per_root) {
             if (tn.hash_pairs) count_kernel<true, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
             else if (P.intersect) count_kernel<true, false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+            else if (halo_parts) count_kernel<true, false, false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
             else count_kernel<true, false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
         } else {
             if (tn.hash_pairs) count_kernel<false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
             else if (P.intersect) count_kernel<false, false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+            else if (halo_parts) count_kernel<false, false, false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
             else count_kernel<false, false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
         }
         if (kev) TC_TRY(record_kernel_event(kev[1], s));

@@ -151,9 +151,12 @@ int launch_flat(const int32_t *rp, const int32_t *col, int64_t n_roots, int max_
                 unsigned long long *result, unsigned long long *per_root, const Tuned &tn, cudaStream_t s,
                 int *launches, cudaEvent_t *kev);
 
+// halo_parts: some graph of the launch is a halo part (n_roots < n_rows); its
+// heavy units then run the count kernel's instance for small units.
 int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, int64_t total_vertices,
                  int64_t max_rows, const CountScratch &sc, CountWork *work, unsigned long long *results, bool per_root,
-                 const Tuned &tn, cudaStream_t s, int *launches, cudaEvent_t *kev = nullptr);
+                 const Tuned &tn, cudaStream_t s, int *launches, cudaEvent_t *kev = nullptr,
+                 bool halo_parts = false);
 
 // ---- scans and sort (tc_scan.cu, tc_sort.cu) ----------------------------------------
 // Exclusive scan of n values into out[0..n] (out[n] = total).  out may alias in.
