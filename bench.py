@@ -664,6 +664,26 @@ def run_parts(args, world, rank, local, pg):
                                                                     row["count"]["batched_ms"])
             per_k[str(k)] = row
         detail["parts"] = per_k
+        # the same graph on balanced label-propagation parts (the stand-in for
+        # the reference's METIS assignment), k = 8, counting halo, batched
+        t0 = time.perf_counter()
+        lp_part = ctx.parts_lp(ug, 8)
+        lp_s = time.perf_counter() - t0
+        rp_u, col_u, _ = ug.download()
+        rows_u = np.repeat(np.arange(len(rp_u) - 1, dtype=np.int64), np.diff(rp_u))
+        cut = float((lp_part[rows_u] != lp_part[col_u]).mean())
+        del rows_u, rp_u, col_u
+        lp_parts = ctx.halo_extract(ug, lp_part, 8, mode="count")
+        lb = ctx.batch(lp_parts)
+        assert int(lb.run().sum()) == whole
+        lp_ms, _ = timed(lambda: lb.run_async())
+        assert int(lb.results().sum()) == whole
+        detail["lp_parts_k8"] = {"partition_s": lp_s, "cut_fraction": cut,
+                                 "max_part_over_mean": float(np.bincount(lp_part).max() * 8 / V),
+                                 "parts_nnz_over_graph": sum(p.nnz for p in lp_parts) / E, "batched_ms": mean(lp_ms),
+                                 "note": "balanced label propagation on the device (tc_gen_parts_lp), counting halo"}
+        lb.free()
+        del lp_parts
         parts, b, b_ms, b_k = head
         ms = mean(b_ms)
         launches = b.stats()["launches"]

@@ -275,7 +275,9 @@ void prep_loop(tc_server *s, int li) {
         const size_t bytes = tc::graph_device_bytes(g);
         s->used += bytes;
         r->g = g;
-        if (r->key) {
+        // a key already made resident meanwhile (the other lane built it for a
+        // request of another size) keeps its graph; this one is the request's own
+        if (r->key && s->cache.count(r->key) == 0) {
             Resident &res = s->cache[r->key];
             res.g = g;
             res.bytes = bytes;
