@@ -232,9 +232,14 @@ TC_API int tc_batch_stats(tc_batch *b, tc_count_stats *stats);
 /* The partitioned drop-in from host memory: the parts of one graph (the
  * u64 blocks that wo_sort_tc_256 reads, narrowed to int32 by the caller, or
  * int32 parts from tc_halo_extract / the .tcsr cache) are uploaded and
- * validated, counted together in one batched launch, and outs[p] (and
- * *total, may be NULL) returned.  Replaces the per-part cudaMalloc / copy /
- * launch / read-back loop of without_sorting_tc.cu:244-465. */
+ * validated, counted, and outs[p] (and *total, may be NULL) returned.  All
+ * uploads go out at once on a copy stream; a few large parts (at most 64,
+ * 4 M entries each on average) are counted one launch each as soon as each is
+ * uploaded and validated, overlapping the remaining uploads; many small
+ * graphs are counted together in one batched launch.  Host arrays should be
+ * page-locked (tc_host_alloc_pinned) for the copies to overlap.  Replaces the
+ * per-part cudaMalloc / copy / launch / read-back loop of
+ * without_sorting_tc.cu:244-465. */
 TC_API int tc_count_parts_csr_i32(tc_ctx *ctx, int n_parts, const int32_t *const *row_ptrs,
                                   const int32_t *const *cols, const int64_t *n_rows, const int64_t *nnz,
                                   const int64_t *n_roots, uint64_t *outs, uint64_t *total);

@@ -85,3 +85,28 @@ def test_parts_from_host_rejects_a_bad_part(ctx):
     with pytest.raises(tc.TCError) as e:
         ctx.count_parts_csr([(rp, np.array([1, 2, 2], np.int32), 3), (rp, bad, 3)])
     assert e.value.code == "TC_E_FORMAT"
+
+
+def test_parts_from_host_overlapped_uploads(ctx):
+    """Large parts (over 4 M entries each) take the overlapped path: every
+    upload goes out at once and each part is counted as soon as it is in and
+    validated.  Counts equal the batched launch's and sum to the whole graph;
+    a corrupt large part is still refused with TC_E_FORMAT."""
+    import trianglecount_gb300 as tc
+    src, dst = gen.rmat(20)
+    ug = ctx.ugraph_from_edges(src, dst)
+    whole = ctx.count(ctx.orient(ug))
+    parts = ctx.halo_extract(ug, gen.parts_random(ug.info()[0], 2), 2, mode="count")
+    host = [(*p.download(), p.n_roots) for p in parts]
+    assert min(len(h[1]) for h in host) >= (1 << 22)
+    want = [int(x) for x in ctx.batch(parts).run()]
+    for _ in range(2):
+        assert [int(x) for x in ctx.count_parts_csr(host)] == want
+    assert sum(want) == whole
+    rp1, col1, r1 = host[1]
+    bad = col1.copy()
+    bad[len(bad) // 2] = len(rp1) + 5  # an id out of range
+    with pytest.raises(tc.TCError) as e:
+        ctx.count_parts_csr([host[0], (rp1, bad, r1)])
+    assert e.value.code == "TC_E_FORMAT"
+    assert [int(x) for x in ctx.count_parts_csr(host)] == want  # the context is still usable

@@ -204,6 +204,9 @@ struct tc_ctx {
     cudaEvent_t kev[2] = {nullptr, nullptr};  // around the last count kernel launch
     bool kev_recorded = false;
     unsigned long long *h_pinned = nullptr;  // small pinned read-back area
+    // created on first use by tc_count_parts_csr_i32: a copy stream and a
+    // high-priority validation stream, so uploads overlap the counts
+    cudaStream_t aux[2] = {nullptr, nullptr};
     std::atomic<int> refs{1};                // the handle + one per live object
 };
 
