@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-ref-kernel", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default thresholds (no autotuning)")
+    ap.add_argument("--tuning", default="", help='plain workloads: fixed thresholds as JSON (e.g. \'{"intersect": 2}\'), '
+                                             'instead of autotuning')
     return ap.parse_args()
 
 
@@ -285,7 +287,9 @@ def run_ours(args, world, rank, local, pg):
     ug_rows, ug_nnz = ug.info()
     ug.free()
     tuning, tune_ms = ({}, None)
-    if not args.no_tune:  # per-graph strategy thresholds, picked on the device before timing
+    if args.tuning:  # fixed thresholds (profiling an alternative strategy)
+        ctx.set_tuning(**json.loads(args.tuning))
+    elif not args.no_tune:  # per-graph strategy thresholds, picked on the device before timing
         t0 = time.perf_counter()
         tuning, tune_ms = ctx.autotune(g, max_trials=40)
         cfg["autotune_s"] = round(time.perf_counter() - t0, 3)

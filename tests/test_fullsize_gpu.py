@@ -46,19 +46,31 @@ def test_road_flat_and_chain(ctx, full):
         ctx.set_tuning(flat_max_deg=old["flat_max_deg"])
 
 
-def test_rmat23_halo_parts_sum_to_whole(ctx, full):
+@pytest.mark.parametrize("mode", ["reference", "count"])
+def test_rmat23_halo_parts_sum_to_whole(ctx, full, mode):
+    """R-MAT 23's k = 2, 4, 8 parts, in the reference's halo and in the
+    counting halo: per-part launches and the batched launch agree part by
+    part and sum to the oracle's count of the whole graph; the counting
+    parts are no larger and count the same per part."""
     want = full["rmat23"]
     ug = ctx.ugraph_from_edges(*gen.rmat(23, 16))
     og = ctx.orient(ug)
     assert (og.n_rows, og.nnz) == (want["V"], want["oriented_nnz"])
     assert ctx.count(og) == want["triangles"]
     for k in (2, 4, 8):
-        parts = ctx.halo_extract(ug, gen.parts_random(og.n_rows, k), k)
+        part = gen.parts_random(og.n_rows, k)
+        parts = ctx.halo_extract(ug, part, k, mode=mode)
         each = ctx.count_each(parts)
         assert int(each.sum()) == want["triangles"], k
         b = ctx.batch(parts)
         assert np.array_equal(b.run(), each), k
         b.free()
+        if mode == "count":
+            ref = ctx.halo_extract(ug, part, k)
+            assert all(c.nnz <= r.nnz and c.n_roots == r.n_roots for c, r in zip(parts, ref)), k
+            assert np.array_equal(ctx.count_each(ref), each), k
+            for p in ref:
+                p.free()
         for p in parts:
             p.free()
 
