@@ -715,23 +715,40 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
                 wmask[2 * (c - c0)] = mm;
                 wmask[2 * (c - c0) + 1] = lm;
             }
-            unsigned hm = __ballot_sync(kFull, hv);
-            while (hm) {
-                const int k = __ffs(hm) - 1;
-                hm &= hm - 1u;
-                if (lane == k) {
+            // the chunk's heavy tasks in one append: a warp scan of their
+            // units and one packed 64-bit atomic for the chunk, so entries stay
+            // contiguous and sorted by unit.  (One atomic per heavy task on the
+            // one hot word serialised the pass when a batch of halo parts holds
+            // hundreds of thousands of heavy tasks.)
+            const unsigned hm = __ballot_sync(kFull, hv);
+            if (hm) {
+                unsigned units = 0;
+                int ns = 0;
+                if (hv) {
                     const int n_part = (x < G.n_roots ? d : 0) + nin;
                     const int max_slices = max(1, (n_part + kHeavyChunk - 1) / kHeavyChunk);
-                    int ns = (int)min((w + unit - 1) / unit, (unsigned long long)max_slices);
+                    ns = (int)min((w + unit - 1) / unit, (unsigned long long)max_slices);
                     ns = max(ns, 1);
-                    const unsigned units = (unsigned)((d + P.tile - 1) / P.tile) * (unsigned)ns;
-                    const unsigned long long base = atomicAdd(&P.work->heavy_packed, (1ull << 32) | units);
-                    const unsigned long long idx = base >> 32;
+                    units = (unsigned)((d + P.tile - 1) / P.tile) * (unsigned)ns;
+                }
+                unsigned incl = units;
+#pragma unroll
+                for (int o = 1; o < kWarp; o <<= 1) {
+                    const unsigned t = __shfl_up_sync(kFull, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                const unsigned chunk_units = __shfl_sync(kFull, incl, kWarp - 1);
+                unsigned long long base = 0;
+                if (lane == 0)
+                    base = atomicAdd(&P.work->heavy_packed, ((unsigned long long)__popc(hm) << 32) | chunk_units);
+                base = __shfl_sync(kFull, base, 0);
+                if (hv) {
+                    const unsigned long long idx = (base >> 32) + (unsigned)__popc(hm & ((1u << lane) - 1u));
                     if ((int64_t)idx < P.heavy_cap) {
                         HeavyEntry e;
                         e.g = g;
                         e.u = (int32_t)x;
-                        e.unit_base = (int32_t)(unsigned)base;
+                        e.unit_base = (int32_t)((unsigned)base + (incl - units));
                         e.n_slices = ns;
                         heavy[idx] = e;
                     } else {
