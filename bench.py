@@ -25,8 +25,8 @@ Printed on rank 0 as ONE JSON line:
   roofline   of the dominant kernel (count_kernel of the batched launch):
              achieved = the bytes this design must read (each root list, each
              edge's row_ptr pair and the cheaper side's list) / its device time;
-             the DRAM traffic of one launch (ncu) and the fixed per-edge model
-             of the survey (every N+(v) read) beside it
+             the DRAM traffic of one launch (ncu) and the every-wedge byte
+             model (every N+(v) read, the reference's probes) beside it
   cpu_baseline  the OpenMP merge-intersection oracle on the machine's host cores,
              one full count of the graph
   reference_gpu_kernel  the reference's own TC_128 kernel (built from its
@@ -747,8 +747,8 @@ def run_parts(args, world, rank, local, pg):
                 "dram_achieved": traffic / sec / 1e9 if traffic else None,
                 "dram_frac": traffic / sec / 1e9 / peak if traffic else None,
                 "traffic_source": (tr or {}).get("source"),
-                "survey_model_bytes": B_model, "survey_model_frac": B_model / sec / 1e9 / peak,
-                "survey_model_note": "4(R+1) + 12 E_R + 4 W+ + 8 per part (every N+(v) read): work the min-side "
+                "wedge_model_bytes": B_model, "wedge_model_frac": B_model / sec / 1e9 / peak,
+                "wedge_model_note": "4(R+1) + 12 E_R + 4 W+ + 8 per part (every N+(v) read): work the min-side "
                                      "design does not do, so its fraction can exceed 1 and is not evidence",
                 "W_plus": W_tot}
 
@@ -935,8 +935,8 @@ def run_batch(args, world, rank, local, pg):
                         "algorithmic_bytes_per_launch": B_min,
                         "algorithmic_bytes_definition": "sum over graphs of 4(V+1) + 12|E+| + 4 sum_{u->v} "
                                                         "min(d+(u), d+(v)) + 8",
-                        "survey_model_bytes": B_model,
-                        "survey_model_frac": B_model / (k_ms / 1000.0) / 1e9 / peak},
+                        "wedge_model_bytes": B_model,
+                        "wedge_model_frac": B_model / (k_ms / 1000.0) / 1e9 / peak},
            "cpu_baseline": {"value": E / cpu_s, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
                             "sample": "all 256 graphs, one OpenMP count each", "seconds": cpu_s,
                             "count_matches": cpu_total == int(outs.sum())}}

@@ -77,7 +77,7 @@ def test_gpu_arm_partitioned_line_is_complete():
     assert d["config"]["workload"] == "rmat16_ef16_halo_parts" and d["value"] > 0 and d["scaling"] == "strong"
     r = d["roofline"]
     assert r["achieved"] > 0 and abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-9
-    assert r["survey_model_bytes"] >= r["algorithmic_bytes_per_launch"] > 0
+    assert r["wedge_model_bytes"] >= r["algorithmic_bytes_per_launch"] > 0
     for k in ("2", "4", "8"):
         row = d["detail"]["parts"][k]
         assert row["count"]["parts_nnz_total"] <= row["reference"]["parts_nnz_total"]
