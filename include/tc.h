@@ -340,7 +340,11 @@ typedef struct tc_server_stats {
 TC_API int tc_server_create(tc_ctx *ctx, const tc_server_config *cfg, tc_server **out);
 /* Queue a count.  graph_key != 0 keeps the oriented graph resident under that
  * key; a later request with the same key is counted without preprocessing (it
- * may then pass no edges).  The edge arrays are copied before returning (into
+ * may then pass no edges).  A key names one graph: requests that give edges
+ * under a key must give the same graph (repeated edges are dropped, so a
+ * longer list of the same edges is the same graph).  If both lanes build one
+ * key at once, the first build becomes the resident graph and the other
+ * serves only its own request.  The edge arrays are copied before returning (into
  * the pinned staging area when it has room). */
 TC_API int tc_server_submit(tc_server *s, uint64_t graph_key, const int64_t *src, const int64_t *dst, int64_t n_edges,
                             int64_t n_nodes, uint64_t *request_id);

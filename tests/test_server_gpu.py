@@ -150,3 +150,22 @@ def test_staging_area_full_or_absent(ctx, staging):
         for _ in range(2):
             ids = [srv.submit(s, d) for s, d in gs]
             assert [srv.wait(i)[0] for i in ids] == alone
+
+
+def test_one_key_built_by_both_lanes_at_once(ctx):
+    """The same key submitted with its edge list (small lane) and with that
+    list repeated 40 times (over 2^20 edges: the large lane; the clean-up
+    drops the repeats, so it is the same graph) builds in both lanes at once.
+    Both count it exactly; one build becomes the resident graph, the other
+    stays the request's own; a key-only request then counts the resident one."""
+    s, d = gen.rmat(14)
+    want = ctx.count(ctx.graph_from_edges(s, d))
+    big_s, big_d = np.tile(s, 40), np.tile(d, 40)
+    assert len(s) <= (1 << 20) < len(big_s)
+    with tc.Server(ctx) as srv:
+        for _ in range(3):
+            ids = [srv.submit(big_s, big_d, key=99), srv.submit(s, d, key=99)]
+            assert [srv.wait(i)[0] for i in ids] == [want, want]
+            assert srv.wait(srv.submit(key=99))[0] == want
+        st = srv.stats()
+    assert st["failed"] == 0 and st["resident_graphs"] == 1
