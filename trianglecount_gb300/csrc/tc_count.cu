@@ -32,9 +32,10 @@
 //              middle-centric or not, count the middle-centric in-edges of v
 //              and their work (one packed atomic), the root-centric work of u,
 //              and the total
-//   split      in-edge counts out of the packed words
-//   scan       in-edge offsets
-//   transpose  per root u, scatter the middle-centric edges into the in-lists;
+//   scan       in-edge offsets, read from the packed words' high halves; each
+//              word's high half becomes the end of the vertex's in-list
+//   transpose  per root u, scatter the middle-centric edges into the in-lists
+//              (one atomic decrement of the packed word gives the slot);
 //              classify each vertex x by d+(x) and its work w(x): micro tasks
 //              (d+(x) <= 8, w(x) <= 128) are listed from the top of the task
 //              list, light tasks (d+(x) <= warp_max, w(x) <= the light bound)
@@ -81,6 +82,8 @@ constexpr int kAuxGrab = 4;     // 32-row chunks an auxiliary-kernel warp takes 
 // One middle-centric in-edge in a packed in_work word.  Both halves stay below
 // 2^31: a vertex has fewer than nnz in-edges, and its in-partners' d+(u) sum to
 // at most nnz < 2^31 (each u counted once), so one 64-bit atomic adds both.
+// After the in-list scan the high half holds in_off + in-edges (at most the
+// launch's pooled nnz, also < 2^31), and the transpose counts it back down.
 constexpr unsigned long long kInEdge = 1ull << 32;
 constexpr int kLightGrab = 4;   // light tasks a count-kernel warp takes per cursor grab (8 in halo parts:
                                 // they hold ~4x the light tasks; R-MAT 23's eight parts 38.14 -> 38.00 ms)
@@ -379,10 +382,10 @@ struct KParams {
     uint32_t *light_list;  // tasks as global rows chunk * 32 + lane: light tasks from entry 0 up,
                            // micro tasks from entry list_cap - 1 down (counts in work->n_tasks)
     int64_t list_cap;      // entries of light_list (the launch's rows: a row is at most one task)
-    int32_t *in_cnt;       // per vertex (pooled): d+ during in_count, then middle-centric in-edges (split from in_work)
-    int32_t *in_off;       // per vertex (pooled) + 1: exclusive scan of in_cnt
-    unsigned long long *in_work;   // per vertex: (in-edges << 32) | sum of d+(u) over its in-partners u;
-                                   // the transpose counts the high half back down
+    int32_t *in_cnt;       // per vertex (pooled): d+, for in_count's gathers
+    int32_t *in_off;       // per vertex (pooled) + 1: exclusive scan of the middle-centric in-edge counts
+    unsigned long long *in_work;   // per vertex: (in-edges << 32) | sum of d+(u) over its in-partners u; the scan
+                                   // adds in_off to the high half, and the transpose counts it back down to in_off
     unsigned long long *out_work;  // per vertex: sum of d+(v) over its out-partners v
     int32_t *in_list;      // in-partner lists, in_off-indexed
     uint8_t *mid;          // per oriented edge (pooled by ebase): 1 = middle-centric
@@ -546,8 +549,10 @@ __device__ __forceinline__ void aux_next(const KParams &P, int k, int lane, bool
 
 // in_count: per root u of a 32-row chunk, per v in N+(u): middle-centric edges
 // (d+(u) < d+(v)) add one in-edge and d+(u) of work to v; the others add d+(v)
-// to u's root-centric work.
-__global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
+// to u's root-centric work.  Both in_count and transpose_classify are held to
+// 40 registers, 6 resident blocks (R-MAT 23's count 36.92 -> 36.87 ms against
+// 48 registers and 5 blocks).
+__global__ void __launch_bounds__(kThreads, 6) in_count_kernel(KParams P) {
     const int lane = threadIdx.x & (kWarp - 1);
     unsigned long long probes = 0;  // this lane's share of sum_{u->v} min(d+(u), d+(v))
     int64_t c, c_end;
@@ -597,16 +602,23 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
                 const int rrs = __shfl_sync(kFull, rs, k);
                 const int rd = __shfl_sync(kFull, d, k);
                 unsigned long long ow = 0;
-                for (int i = lane; i < rd; i += kWarp) {
-                    const int v = __ldg(col + rrs + i);
-                    const int dv = __ldg(P.in_cnt + G.vbase + v);
-                    const bool m = rd < dv;
-                    P.mid[G.ebase + rrs + i] = (uint8_t)m;
-                    if (m) {
-                        atomicAdd(P.in_work + G.vbase + v, kInEdge | (unsigned long long)rd);
-                        probes += (unsigned long long)rd;
-                    } else {
-                        ow += (unsigned long long)dv;
+                for (int i0 = lane; i0 < rd; i0 += 4 * kWarp) {  // four edges' loads in flight
+                    int v[4], dv[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) v[q] = i0 + q * kWarp < rd ? __ldg(col + rrs + i0 + q * kWarp) : -1;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) dv[q] = v[q] >= 0 ? __ldg(P.in_cnt + G.vbase + v[q]) : 0;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        if (v[q] < 0) continue;
+                        const bool m = rd < dv[q];
+                        P.mid[G.ebase + rrs + i0 + q * kWarp] = (uint8_t)m;
+                        if (m) {
+                            atomicAdd(P.in_work + G.vbase + v[q], kInEdge | (unsigned long long)rd);
+                            probes += (unsigned long long)rd;
+                        } else {
+                            ow += (unsigned long long)dv[q];
+                        }
                     }
                 }
                 probes += ow;
@@ -621,7 +633,7 @@ __global__ void __launch_bounds__(kThreads) in_count_kernel(KParams P) {
 }
 
 // in_cnt[vbase + x] = d+(x) for every row, for in_count's gathers (one load
-// per edge instead of a row_ptr pair); in_cnt is free until the split below.
+// per edge instead of a row_ptr pair).
 __global__ void __launch_bounds__(kThreads) degree_kernel(KParams P) {
     const int lane = threadIdx.x & (kWarp - 1);
     const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
@@ -633,19 +645,33 @@ __global__ void __launch_bounds__(kThreads) degree_kernel(KParams P) {
     }
 }
 
-// in_cnt[i] = the in-edge count (high half) of the packed in_work[i], for the scan.
-__global__ void __launch_bounds__(kThreads) split_in_count_kernel(const unsigned long long *__restrict__ in_work,
-                                                                  int32_t *__restrict__ in_cnt, int64_t n) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-        in_cnt[i] = (int32_t)(in_work[i] >> 32);
+// The transpose's scatter of up to four middle-centric edges i0 + q * step
+// (q < 4, i < d) of root u's row.  The in-list scan left the end of v's
+// in-list in in_work[v]'s high half, so one atomic decrement per edge returns
+// its slot (no in_off gather); the four are issued together, so a lane waits
+// on one L2 round trip per four edges, not one chain per edge.
+__device__ __forceinline__ void scatter4(const KParams &P, const GraphDesc &G, const int32_t *__restrict__ row,
+                                         int64_t e0, int i0, int step, int d, int32_t u) {
+    int v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int i = i0 + q * step;
+        v[q] = i < d && P.mid[e0 + i] ? __ldg(row + i) : -1;
+    }
+    int slot[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        slot[q] = v[q] >= 0 ? (int)(atomicAdd(P.in_work + G.vbase + v[q], 0ull - kInEdge) >> 32) - 1 : 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        if (v[q] >= 0) P.in_list[slot[q]] = u;
 }
 
 // transpose + classify: scatter the chunk's middle-centric edges into the
 // in-lists, then classify each row of the chunk as a micro task (task list,
 // from the top), a light task (task list, from the bottom), a heavy task
 // (block units) or no work.
-__global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P, HeavyEntry *heavy) {
+__global__ void __launch_bounds__(kThreads, 6) transpose_classify_kernel(KParams P, HeavyEntry *heavy) {
     const int lane = threadIdx.x & (kWarp - 1);
     // Block-unit size: unit_work, or less on a small job so that every count
     // block gets about four units; the light-task bound likewise, so that a
@@ -684,12 +710,8 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
             // scatter the middle-centric out-edges of the chunk's roots (marked by
             // in_count): short rows one per lane ...
             if (d >= 1 && d <= kLaneRowDeg && x < G.n_roots) {
-                for (int i = 0; i < d; ++i) {
-                    if (!P.mid[G.ebase + rs + i]) continue;
-                    const int v = __ldg(col + rs + i);
-                    const int pos = (int)(atomicAdd(P.in_work + G.vbase + v, 0ull - kInEdge) >> 32) - 1;
-                    P.in_list[P.in_off[G.vbase + v] + pos] = (int32_t)x;
-                }
+                for (int i0 = 0; i0 < d; i0 += 4)
+                    scatter4(P, G, col + rs, G.ebase + rs, i0, 1, d, (int32_t)x);
             }
             // ... long rows by the whole warp
             unsigned todo = __ballot_sync(kFull, d > kLaneRowDeg && x < G.n_roots);
@@ -698,12 +720,8 @@ __global__ void __launch_bounds__(kThreads) transpose_classify_kernel(KParams P,
                 todo &= todo - 1u;
                 const int rrs = __shfl_sync(kFull, rs, k);
                 const int rd = __shfl_sync(kFull, d, k);
-                for (int i = lane; i < rd; i += kWarp) {
-                    if (!P.mid[G.ebase + rrs + i]) continue;
-                    const int v = __ldg(col + rrs + i);
-                    const int pos = (int)(atomicAdd(P.in_work + G.vbase + v, 0ull - kInEdge) >> 32) - 1;
-                    P.in_list[P.in_off[G.vbase + v] + pos] = (int32_t)(x0 + k);
-                }
+                for (int i0 = lane; i0 < rd; i0 += 4 * kWarp)
+                    scatter4(P, G, col + rrs, G.ebase + rrs, i0, kWarp, rd, (int32_t)(x0 + k));
             }
             // classify
             const bool has = w > 0 && d >= 1;
@@ -1499,6 +1517,12 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     return TC_OK;
 }
 
+// Launches of one scan of n values: one tile, or reduce + the tile sums' scan + scan.
+static int scan_launches(int64_t n) {
+    constexpr int64_t kScanTile = 4096;
+    return n <= kScanTile ? 1 : 2 + scan_launches((n + kScanTile - 1) / kScanTile);
+}
+
 // Records a kernel-timing event on s; inside a stream capture (the plain
 // count's cached graph) as an external event node, so that every replay of
 // the captured chain records it too.
@@ -1561,10 +1585,7 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
         TC_CUDA(cudaGetLastError());
         in_count_kernel<<<aux_blocks, kThreads, 0, s>>>(P);
         TC_CUDA(cudaGetLastError());
-        split_in_count_kernel<<<(int)std::min<int64_t>((total_vertices + kThreads - 1) / kThreads, (int64_t)tn.blocks * 4),
-                                kThreads, 0, s>>>(sc.in_work, sc.in_cnt, total_vertices);
-        TC_CUDA(cudaGetLastError());
-        TC_TRY(scan_exclusive_i32(sc.in_cnt, sc.in_off, total_vertices, s));
+        TC_TRY(scan_in_slots(sc.in_work, sc.in_off, total_vertices, nullptr, 0, s));
         transpose_classify_kernel<<<aux_blocks, kThreads, 0, s>>>(P, sc.heavy);
         TC_CUDA(cudaGetLastError());
         if (per_root) micro_kernel<true><<<aux_blocks, kThreads, 0, s>>>(P);
@@ -1590,7 +1611,7 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
         }
         if (kev) TC_TRY(record_kernel_event(kev[1], s));
         TC_CUDA(cudaGetLastError());
-        nl += 6 + (total_vertices > 4096 ? 3 : 1);
+        nl += 5 + scan_launches(total_vertices);
     }
     if (launches) *launches = nl;
     return TC_OK;
@@ -1667,10 +1688,7 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
         TC_CUDA(cudaGetLastError());
         in_count_kernel<<<aux_blocks, kThreads, 0, s>>>(P);
         TC_CUDA(cudaGetLastError());
-        split_in_count_kernel<<<(int)std::min<int64_t>((total_vertices + kThreads - 1) / kThreads, (int64_t)tn.blocks * 4),
-                                kThreads, 0, s>>>(sc.in_work, sc.in_cnt, total_vertices);
-        TC_CUDA(cudaGetLastError());
-        TC_TRY(scan_exclusive_i32_tmp(sc.in_cnt, sc.in_off, total_vertices, scan_tmp, scan_tmp_cap, s));
+        TC_TRY(scan_in_slots(sc.in_work, sc.in_off, total_vertices, scan_tmp, scan_tmp_cap, s));
         transpose_classify_kernel<<<aux_blocks, kThreads, 0, s>>>(P, sc.heavy);
         TC_CUDA(cudaGetLastError());
         micro_kernel<false><<<aux_blocks, kThreads, 0, s>>>(P);

@@ -167,6 +167,13 @@ int scan_flags_u8(const uint8_t *flags, int32_t *out, int64_t n, cudaStream_t s)
 // scan_exclusive_i32 with its tile sums in caller memory (no allocation).
 int scan_exclusive_i32_tmp(const int32_t *in, int32_t *out, int64_t n, int32_t *tmp, int64_t tmp_cap,
                            cudaStream_t s);
+// The count's in-list offsets: in_off[0..n] = exclusive scan of the in-edge
+// counts held in the high halves of in_work[0..n), and each in_work[i]'s high
+// half becomes in_off[i] + count, the end of vertex i's in-list.  The tile
+// sums go to tmp (tmp_cap values), or to a stream-ordered allocation when tmp
+// is null.
+int scan_in_slots(unsigned long long *in_work, int32_t *in_off, int64_t n, int32_t *tmp, int64_t tmp_cap,
+                  cudaStream_t s);
 // LSD radix sort of n 64-bit keys on bits [0, bits).  Result in *keys (the
 // two buffers may be swapped).  tmp must hold n keys.
 int radix_sort_u64(uint64_t **keys, uint64_t **tmp, int64_t n, int bits, cudaStream_t s);

@@ -21,6 +21,13 @@ constexpr int kItems = 16;        // values per thread
 constexpr int kTile = kT * kItems;
 constexpr unsigned kFull = 0xffffffffu;
 
+// Scan input: the high halves of packed 64-bit words (the count kernel's
+// in-edge counts in its in_work words).
+struct HighHalf {
+    const unsigned long long *p;
+    __device__ __forceinline__ int32_t operator[](int64_t i) const { return (int32_t)(p[i] >> 32); }
+};
+
 template <class T>
 __device__ __forceinline__ T warp_incl_scan(T v, int lane) {
 #pragma unroll
@@ -52,8 +59,9 @@ __device__ __forceinline__ T block_excl_scan(T v, T *total) {
     return before + incl - v;
 }
 
+// The scans read their input through In: a plain pointer, or HighHalf below.
 template <class In, class Out>
-__global__ void __launch_bounds__(kT) tile_reduce_kernel(const In *in, int64_t n, Out *tile_sums) {
+__global__ void __launch_bounds__(kT) tile_reduce_kernel(In in, int64_t n, Out *tile_sums) {
     const int64_t base = (int64_t)blockIdx.x * kTile;
     Out s = 0;
 #pragma unroll
@@ -67,9 +75,11 @@ __global__ void __launch_bounds__(kT) tile_reduce_kernel(const In *in, int64_t n
 }
 
 // Exclusive scan of each tile plus the tile's offset; out[n] gets the total
-// when the last tile is processed (tile_off has n_tiles + 1 entries).
+// when the last tile is processed (tile_off has n_tiles + 1 entries).  With
+// slots set, slots[i] also gets out[i] added to its high half.
 template <class In, class Out>
-__global__ void __launch_bounds__(kT) tile_scan_kernel(const In *in, int64_t n, const Out *tile_off, Out *out) {
+__global__ void __launch_bounds__(kT) tile_scan_kernel(In in, int64_t n, const Out *tile_off, Out *out,
+                                                       unsigned long long *slots) {
     const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kItems;  // blocked layout
     Out v[kItems];
     Out s = 0;
@@ -84,7 +94,10 @@ __global__ void __launch_bounds__(kT) tile_scan_kernel(const In *in, int64_t n, 
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         const int64_t i = base + k;
-        if (i < n) out[i] = run;
+        if (i < n) {
+            out[i] = run;
+            if (slots) slots[i] += (unsigned long long)run << 32;
+        }
         run += v[k];
     }
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = tile_off[gridDim.x];
@@ -92,7 +105,7 @@ __global__ void __launch_bounds__(kT) tile_scan_kernel(const In *in, int64_t n, 
 
 // One-tile scan (n <= kTile): out[0..n) exclusive, out[n] = total.
 template <class In, class Out>
-__global__ void __launch_bounds__(kT) single_tile_scan_kernel(const In *in, int64_t n, Out *out) {
+__global__ void __launch_bounds__(kT) single_tile_scan_kernel(In in, int64_t n, Out *out, unsigned long long *slots) {
     const int64_t base = (int64_t)threadIdx.x * kItems;
     Out v[kItems];
     Out s = 0;
@@ -107,21 +120,24 @@ __global__ void __launch_bounds__(kT) single_tile_scan_kernel(const In *in, int6
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         const int64_t i = base + k;
-        if (i < n) out[i] = run;
+        if (i < n) {
+            out[i] = run;
+            if (slots) slots[i] += (unsigned long long)run << 32;
+        }
         run += v[k];
     }
     if (threadIdx.x == 0) out[n] = tot;
 }
 
 template <class In, class Out>
-int scan_impl(const In *in, Out *out, int64_t n, cudaStream_t s) {
+int scan_impl(In in, Out *out, int64_t n, cudaStream_t s, unsigned long long *slots = nullptr) {
     if (n <= 0) {
         TC_CUDA(cudaMemsetAsync(out, 0, sizeof(Out), s));
         return TC_OK;
     }
     const int64_t tiles = (n + kTile - 1) / kTile;
     if (tiles == 1) {
-        single_tile_scan_kernel<In, Out><<<1, kT, 0, s>>>(in, n, out);
+        single_tile_scan_kernel<In, Out><<<1, kT, 0, s>>>(in, n, out, slots);
         TC_CUDA(cudaGetLastError());
         return TC_OK;
     }
@@ -130,8 +146,8 @@ int scan_impl(const In *in, Out *out, int64_t n, cudaStream_t s) {
     tile_reduce_kernel<In, Out><<<(unsigned)tiles, kT, 0, s>>>(in, n, sums.p);
     TC_CUDA(cudaGetLastError());
     // exclusive scan of the tile sums in place (recursion ends at one tile)
-    TC_TRY((scan_impl<Out, Out>(sums.p, sums.p, tiles, s)));
-    tile_scan_kernel<In, Out><<<(unsigned)tiles, kT, 0, s>>>(in, n, sums.p, out);
+    TC_TRY((scan_impl<const Out *, Out>(sums.p, sums.p, tiles, s)));
+    tile_scan_kernel<In, Out><<<(unsigned)tiles, kT, 0, s>>>(in, n, sums.p, out, slots);
     TC_CUDA(cudaGetLastError());
     return TC_OK;
 }
@@ -221,22 +237,23 @@ __global__ void __launch_bounds__(kT) radix_scatter_kernel(const uint64_t *keys,
 
 // Same scan with the tile sums of every recursion level in tmp (tmp_cap values).
 template <class In, class Out>
-int scan_tmp_impl(const In *in, Out *out, int64_t n, Out *tmp, int64_t tmp_cap, cudaStream_t s) {
+int scan_tmp_impl(In in, Out *out, int64_t n, Out *tmp, int64_t tmp_cap, cudaStream_t s,
+                  unsigned long long *slots = nullptr) {
     if (n <= 0) {
         TC_CUDA(cudaMemsetAsync(out, 0, sizeof(Out), s));
         return TC_OK;
     }
     const int64_t tiles = (n + kTile - 1) / kTile;
     if (tiles == 1) {
-        single_tile_scan_kernel<In, Out><<<1, kT, 0, s>>>(in, n, out);
+        single_tile_scan_kernel<In, Out><<<1, kT, 0, s>>>(in, n, out, slots);
         TC_CUDA(cudaGetLastError());
         return TC_OK;
     }
     if (tiles + 1 > tmp_cap) return set_error(TC_E_RANGE, "scan temp of %lld values is too small", (long long)tmp_cap);
     tile_reduce_kernel<In, Out><<<(unsigned)tiles, kT, 0, s>>>(in, n, tmp);
     TC_CUDA(cudaGetLastError());
-    TC_TRY((scan_tmp_impl<Out, Out>(tmp, tmp, tiles, tmp + tiles + 1, tmp_cap - (tiles + 1), s)));
-    tile_scan_kernel<In, Out><<<(unsigned)tiles, kT, 0, s>>>(in, n, tmp, out);
+    TC_TRY((scan_tmp_impl<const Out *, Out>(tmp, tmp, tiles, tmp + tiles + 1, tmp_cap - (tiles + 1), s)));
+    tile_scan_kernel<In, Out><<<(unsigned)tiles, kT, 0, s>>>(in, n, tmp, out, slots);
     TC_CUDA(cudaGetLastError());
     return TC_OK;
 }
@@ -245,17 +262,23 @@ int scan_tmp_impl(const In *in, Out *out, int64_t n, Out *tmp, int64_t tmp_cap, 
 
 int scan_exclusive_i32_tmp(const int32_t *in, int32_t *out, int64_t n, int32_t *tmp, int64_t tmp_cap,
                            cudaStream_t s) {
-    return scan_tmp_impl<int32_t, int32_t>(in, out, n, tmp, tmp_cap, s);
+    return scan_tmp_impl<const int32_t *, int32_t>(in, out, n, tmp, tmp_cap, s);
 }
 
 int scan_exclusive_i32(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s) {
-    return scan_impl<int32_t, int32_t>(in, out, n, s);
+    return scan_impl<const int32_t *, int32_t>(in, out, n, s);
 }
 int scan_exclusive_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s) {
-    return scan_impl<int64_t, int64_t>(in, out, n, s);
+    return scan_impl<const int64_t *, int64_t>(in, out, n, s);
 }
 int scan_flags_u8(const uint8_t *flags, int32_t *out, int64_t n, cudaStream_t s) {
-    return scan_impl<uint8_t, int32_t>(flags, out, n, s);
+    return scan_impl<const uint8_t *, int32_t>(flags, out, n, s);
+}
+int scan_in_slots(unsigned long long *in_work, int32_t *in_off, int64_t n, int32_t *tmp, int64_t tmp_cap,
+                  cudaStream_t s) {
+    const HighHalf in{in_work};
+    if (tmp) return scan_tmp_impl<HighHalf, int32_t>(in, in_off, n, tmp, tmp_cap, s, in_work);
+    return scan_impl<HighHalf, int32_t>(in, in_off, n, s, in_work);
 }
 
 int radix_sort_u64(uint64_t **keys, uint64_t **tmp, int64_t n, int bits, cudaStream_t s) {
