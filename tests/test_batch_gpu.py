@@ -110,3 +110,18 @@ def test_parts_from_host_overlapped_uploads(ctx):
         ctx.count_parts_csr([host[0], (rp1, bad, r1)])
     assert e.value.code == "TC_E_FORMAT"
     assert [int(x) for x in ctx.count_parts_csr(host)] == want  # the context is still usable
+
+
+def test_batch_over_int32_pooled_edges_is_refused(ctx):
+    """A launch pools its graphs' in-list offsets as int32: one graph listed
+    often enough to pass 2^31 - 1 oriented edges in total is refused with
+    TC_E_RANGE before anything is allocated, and the context stays usable."""
+    import trianglecount_gb300 as tc
+    src, dst = gen.rmat(18)
+    orp, ocl, t = oracle.pipeline(src, dst)
+    g = ctx.upload(orp, ocl)
+    n = (1 << 31) // g.nnz + 1
+    with pytest.raises(tc.TCError) as e:
+        ctx.batch([g] * n)
+    assert e.value.code == "TC_E_RANGE"
+    assert list(ctx.batch([g] * 3).run()) == [t, t, t]

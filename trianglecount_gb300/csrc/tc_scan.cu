@@ -3,8 +3,9 @@
 // cub::DeviceScan::InclusiveSum, cub::DeviceMergeSort and cub::DeviceSelect
 // for these steps: without_part_preprocess.py:256, round_clean_subgraph.cu:468-495, 561-567).
 //
-// Scan: reduce-then-scan over tiles of 4096 values (256 threads x 16), the
-// tile sums scanned recursively.  Radix sort: 8-bit digits, per pass
+// Scan: reduce-then-scan over tiles of 4096 values (256 threads x 16, each
+// warp scanning runs of 32 consecutive values, so every access is
+// coalesced), the tile sums scanned recursively.  Radix sort: 8-bit digits, per pass
 // (1) per-tile digit histograms, (2) one exclusive scan over the
 // digit-major histogram table, (3) a stable scatter in which each warp ranks
 // its contiguous 512-key segment with __match_any_sync and the block stages
@@ -74,58 +75,63 @@ __global__ void __launch_bounds__(kT) tile_reduce_kernel(In in, int64_t n, Out *
     if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
 }
 
-// Exclusive scan of each tile plus the tile's offset; out[n] gets the total
-// when the last tile is processed (tile_off has n_tiles + 1 entries).  With
-// slots set, slots[i] also gets out[i] added to its high half.
+// Exclusive scan of one tile [base, base + kTile) in a warp-striped layout:
+// warp w owns kItems runs of 32 consecutive values, so every load and store
+// of a warp is one coalesced 32-value access.  Values are held in registers
+// between the warp totals' block scan and the per-run warp scans, so out may
+// alias in.  out[i] = off + the tile's exclusive prefix; with slots set,
+// slots[i] also gets out[i] added to its high half.  Returns the tile total.
 template <class In, class Out>
-__global__ void __launch_bounds__(kT) tile_scan_kernel(In in, int64_t n, const Out *tile_off, Out *out,
-                                                       unsigned long long *slots) {
-    const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kItems;  // blocked layout
+__device__ __forceinline__ Out scan_tile_striped(In in, int64_t n, int64_t base, Out off, Out *out,
+                                                 unsigned long long *slots) {
+    __shared__ Out warp_tot[kT / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t wb = base + (int64_t)w * (kItems * 32);
     Out v[kItems];
     Out s = 0;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
-        const int64_t i = base + k;
+        const int64_t i = wb + k * 32 + lane;
         v[k] = i < n ? (Out)in[i] : Out(0);
         s += v[k];
     }
-    Out tot;
-    Out run = block_excl_scan<Out>(s, &tot) + tile_off[blockIdx.x];
+    s = __shfl_sync(kFull, warp_incl_scan(s, lane), 31);
+    if (lane == 0) warp_tot[w] = s;
+    __syncthreads();
+    Out run = off, tot = 0;
+#pragma unroll
+    for (int j = 0; j < kT / 32; ++j) {
+        const Out t = warp_tot[j];
+        run += j < w ? t : Out(0);
+        tot += t;
+    }
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
-        const int64_t i = base + k;
+        const Out incl = warp_incl_scan(v[k], lane);
+        const int64_t i = wb + k * 32 + lane;
         if (i < n) {
-            out[i] = run;
-            if (slots) slots[i] += (unsigned long long)run << 32;
+            const Out x = run + incl - v[k];
+            out[i] = x;
+            if (slots) slots[i] += (unsigned long long)x << 32;
         }
-        run += v[k];
+        run += __shfl_sync(kFull, incl, 31);
     }
+    return tot;
+}
+
+// Exclusive scan of each tile plus the tile's offset; out[n] gets the total
+// when the last tile is processed (tile_off has n_tiles + 1 entries).
+template <class In, class Out>
+__global__ void __launch_bounds__(kT) tile_scan_kernel(In in, int64_t n, const Out *tile_off, Out *out,
+                                                       unsigned long long *slots) {
+    scan_tile_striped<In, Out>(in, n, (int64_t)blockIdx.x * kTile, tile_off[blockIdx.x], out, slots);
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = tile_off[gridDim.x];
 }
 
 // One-tile scan (n <= kTile): out[0..n) exclusive, out[n] = total.
 template <class In, class Out>
 __global__ void __launch_bounds__(kT) single_tile_scan_kernel(In in, int64_t n, Out *out, unsigned long long *slots) {
-    const int64_t base = (int64_t)threadIdx.x * kItems;
-    Out v[kItems];
-    Out s = 0;
-#pragma unroll
-    for (int k = 0; k < kItems; ++k) {
-        const int64_t i = base + k;
-        v[k] = i < n ? (Out)in[i] : Out(0);
-        s += v[k];
-    }
-    Out tot;
-    Out run = block_excl_scan<Out>(s, &tot);
-#pragma unroll
-    for (int k = 0; k < kItems; ++k) {
-        const int64_t i = base + k;
-        if (i < n) {
-            out[i] = run;
-            if (slots) slots[i] += (unsigned long long)run << 32;
-        }
-        run += v[k];
-    }
+    const Out tot = scan_tile_striped<In, Out>(in, n, 0, Out(0), out, slots);
     if (threadIdx.x == 0) out[n] = tot;
 }
 
