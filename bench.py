@@ -778,7 +778,9 @@ def run_parts(args, world, rank, local, pg):
             "config": cfg, "gpu_launches": launches * args.steps,
             "e2e": {"value": E / (e2e / 1000.0) if e2e else None, "unit": UNIT, "ms_per_step": e2e,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 20 * len(pinned) + 48,
-                    "path": "tc_count_parts_csr_i32: upload + validate every part, one batched count, read-back"},
+                    "path": "tc_count_parts_csr_i32: every part's upload issued at once; each part validated "
+                            "and counted (one launch per part) as soon as it is in, under the later uploads; "
+                            "read-back"},
             "roofline": roofline, "clocks": clk, "detail": detail,
         }
         if world == 1 and not args.no_ref_kernel:
