@@ -121,7 +121,7 @@ TC_API int tc_ctx_device_info(tc_ctx *ctx, int *sm_count, size_t *free_bytes, si
 typedef struct tc_tuning {
     int32_t warp_max_deg;   /* 32..512, power of two */
     int32_t light_max_work; /* wedge probes a light task may have */
-    int32_t unit_work;      /* target wedge probes per heavy block unit */
+    int32_t unit_work;      /* target wedge probes per heavy block unit (default 2^20) */
     int32_t long_list;      /* 0..4096 */
     int32_t probe_kicks;    /* 0..1024 */
     int32_t heavy_bitmap;   /* 0 or 1 */

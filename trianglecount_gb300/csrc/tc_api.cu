@@ -619,7 +619,7 @@ int tc_ctx_create(int device, tc_ctx **out) {
     c->sm_count = device_sm_count(device);
     c->tuning.warp_max_deg = 256;
     c->tuning.light_max_work = 8192;
-    c->tuning.unit_work = 262144;
+    c->tuning.unit_work = 1048576;
     c->tuning.long_list = 32;
     c->tuning.probe_kicks = 32;
     c->tuning.heavy_bitmap = 0;  // an autotuner candidate: one 32-warp block per SM rarely pays off

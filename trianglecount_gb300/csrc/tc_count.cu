@@ -1453,7 +1453,10 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     r.log_block_slots = pow2_floor_log(block_slots);
     r.tile = block_slots / 4;
     r.light_max_work = t.light_max_work > 0 ? t.light_max_work : 8192;
-    r.unit_work = t.unit_work > 0 ? t.unit_work : 262144;
+    // 2^20 probes per heavy unit: against 2^18, R-MAT 23 36.85 -> 36.10 ms whole and
+    // 40.97 -> 40.65 ms in eight halo parts, R-MAT 21 6.70 -> 6.65 ms (fewer table
+    // builds per hub; the persistent grid's dynamic grabs keep the blocks balanced)
+    r.unit_work = t.unit_work > 0 ? t.unit_work : 1048576;
     r.long_list = t.long_list >= 0 ? t.long_list : 32;
     r.probe_kicks = t.probe_kicks >= 0 ? t.probe_kicks : 32;
     r.heavy_bitmap = t.heavy_bitmap >= 0 ? t.heavy_bitmap : 0;

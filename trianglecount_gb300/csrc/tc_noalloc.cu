@@ -89,7 +89,7 @@ int setup_device(int dev, DeviceSetup **out) {
         tc_tuning t{};
         t.warp_max_deg = 256;
         t.light_max_work = 8192;
-        t.unit_work = 262144;
+        t.unit_work = 1048576;
         t.long_list = 32;
         t.probe_kicks = 32;
         t.heavy_bitmap = 0;  // the allocation-free variant keeps the fixed heavy path

@@ -52,7 +52,7 @@ extern "C" int tc_autotune_ex(tc_ctx *ctx, tc_graph *g, int max_trials, int reps
     const std::vector<int32_t> grid[9] = {
         {64, 128, 256, 512},
         {4096, 8192, 16384, 32768, 65536, 131072},
-        {65536, 131072, 262144, 524288, 1048576},
+        {131072, 262144, 524288, 1048576, 2097152, 4194304},
         {8, 16, 32, 64},
         {0, 32},
         {0, 1},
