@@ -383,12 +383,12 @@ void ctx_release(tc_ctx *c) {
 }
 
 int scratch_alloc(CountScratch *sc, int64_t V, int64_t E, int64_t heavy_cap, cudaStream_t s) {
-    // in-list offsets and slots are int32 over the launch's pooled vertices and edges
-    if (V >= INT32_MAX || E >= INT32_MAX)
+    // in-list offsets and slots are int32 over the launch's pooled edges
+    if (E >= INT32_MAX)
         return set_error(TC_E_RANGE,
-                         "one count launch holds fewer than 2^31 - 1 rows and oriented edges in total, got %lld and "
-                         "%lld: split the batch",
-                         (long long)V, (long long)E);
+                         "one count launch holds fewer than 2^31 - 1 oriented edges in total, got %lld: split the "
+                         "batch",
+                         (long long)E);
     sc->heavy_cap = heavy_cap;
     TC_TRY(dalloc((void **)&sc->heavy, sizeof(HeavyEntry) * (size_t)std::max<int64_t>(heavy_cap, 1), s));
     TC_TRY(dalloc((void **)&sc->light_list, sizeof(uint32_t) * (size_t)std::max<int64_t>(V, 1), s));

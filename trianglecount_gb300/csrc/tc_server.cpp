@@ -300,7 +300,10 @@ void count_loop(tc_server *s, int li) {
         s->cv.wait(lk, [&] { return s->stopping || !L.ready.empty(); });
         if (s->stopping && L.ready.empty()) return;
         std::vector<Request *> batch;
-        while (!L.ready.empty() && (int)batch.size() < s->cfg.max_batch) {
+        int64_t pooled = 0;  // a launch's pooled edges stay below 2^31 - 1 (int32 in-list offsets)
+        while (!L.ready.empty() && (int)batch.size() < s->cfg.max_batch &&
+               (batch.empty() || pooled + L.ready.front()->g->nnz < (int64_t)INT32_MAX)) {
+            pooled += L.ready.front()->g->nnz;
             batch.push_back(L.ready.front());
             L.ready.pop_front();
             batch.back()->state = kCounting;
