@@ -125,3 +125,32 @@ def test_batch_over_int32_pooled_edges_is_refused(ctx):
         ctx.batch([g] * n)
     assert e.value.code == "TC_E_RANGE"
     assert list(ctx.batch([g] * 3).run()) == [t, t, t]
+
+
+def test_parts_from_host_grouped_launches(ctx):
+    """Five large parts take the overlapped path in groups [0], [1, 2],
+    [3, 4] (sizes 1, 2, 4, ..., the last taking the rest): part 0 is counted
+    on its own, the later groups in one pooled launch each.  Counts
+    equal the batched launch's part by part and sum to the whole graph; a
+    corrupt part inside a pooled group is refused with TC_E_FORMAT after
+    part 0's count was already enqueued, and the context stays usable."""
+    import trianglecount_gb300 as tc
+    src, dst = gen.rmat(21)
+    ug = ctx.ugraph_from_edges(src, dst)
+    whole = ctx.count(ctx.orient(ug))
+    parts = ctx.halo_extract(ug, gen.parts_random(ug.info()[0], 5), 5, mode="count")
+    host = [(*p.download(), p.n_roots) for p in parts]
+    assert sum(len(h[1]) for h in host) // len(host) >= (1 << 22)
+    want = [int(x) for x in ctx.batch(parts).run()]
+    for _ in range(2):
+        assert [int(x) for x in ctx.count_parts_csr(host)] == want
+    assert sum(want) == whole
+    for k in (3, 4):  # three parts: groups [0], [1, 2]; four: [0], [1, 2, 3]
+        assert [int(x) for x in ctx.count_parts_csr(host[:k])] == want[:k]
+    rp2, col2, r2 = host[2]
+    bad = col2.copy()
+    bad[len(bad) // 3] = -1  # an id out of range inside the second group
+    with pytest.raises(tc.TCError) as e:
+        ctx.count_parts_csr(host[:2] + [(rp2, bad, r2)] + host[3:])
+    assert e.value.code == "TC_E_FORMAT"
+    assert [int(x) for x in ctx.count_parts_csr(host)] == want

@@ -4,6 +4,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <thread>
 #include <vector>
 
@@ -185,6 +186,16 @@ int ensure_count_scratch(tc_graph *g) {
 }
 
 __global__ void set_desc_kernel(GraphDesc *dst, GraphDesc d) { *dst = d; }
+
+// Up to eight descriptors as one kernel parameter (512 bytes): a table is
+// written in stream order with no host copy (a copy from pageable memory
+// would first wait for the stream to drain).
+struct DescBlock {
+    GraphDesc d[8];
+};
+__global__ void set_descs_kernel(GraphDesc *dst, DescBlock b, int n) {
+    if ((int)threadIdx.x < n) dst[threadIdx.x] = b.d[threadIdx.x];
+}
 
 // The count kernels' error word (CountWork::error) as text.
 const char *count_error_text(int code) {
@@ -1033,6 +1044,65 @@ int tc_batch_stats(tc_batch *b, tc_count_stats *stats) {
     return TC_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// One pooled count launch over a group of parts, enqueued on the context's
+// stream with its results in d_res[0..n); the launch's descriptor table,
+// work words and scratch are freed in stream order when the group goes.
+struct PartGroup {
+    DBuf<GraphDesc> desc;
+    DBuf<CountWork> work;
+    CountScratch sc;
+    cudaStream_t s = nullptr;
+    ~PartGroup() {
+        if (s) scratch_free(&sc, s);
+    }
+};
+
+int enqueue_group_count(tc_ctx *ctx, tc_graph *const *gs, int n, unsigned long long *d_res, PartGroup *grp) {
+    cudaStream_t s = ctx->stream;
+    std::vector<GraphDesc> desc((size_t)n);
+    int64_t chunks = 0, cap = 0, vtot = 0, etot = 0, max_rows = 0;
+    bool halo_parts = false;
+    for (int i = 0; i < n; ++i) {
+        const tc_graph *g = gs[i];
+        max_rows = std::max(max_rows, g->n_rows);
+        halo_parts = halo_parts || g->n_roots < g->n_rows;
+        GraphDesc &d = desc[(size_t)i];
+        memset(&d, 0, sizeof d);
+        d.rp = g->rp;
+        d.col = g->col;
+        d.n_rows = g->n_rows;
+        d.n_roots = g->n_roots;
+        d.chunk_base = chunks;
+        d.vbase = vtot;
+        d.ebase = etot;
+        chunks += (g->n_rows + 31) / 32;
+        vtot += g->n_rows + 1;
+        etot += g->nnz;
+        cap += std::min(g->n_rows, g->nnz) + 1;
+    }
+    grp->s = s;
+    TC_TRY(grp->desc.alloc((size_t)n, s));
+    TC_TRY(grp->work.alloc(1, s));
+    TC_TRY(scratch_alloc(&grp->sc, vtot, etot, cap, s));
+    for (int i0 = 0; i0 < n; i0 += 8) {
+        DescBlock blk;
+        const int m = std::min(8, n - i0);
+        memcpy(blk.d, desc.data() + i0, sizeof(GraphDesc) * (size_t)m);
+        set_descs_kernel<<<1, 8, 0, s>>>(grp->desc.p + i0, blk, m);
+        TC_CUDA(cudaGetLastError());
+    }
+    return launch_count(grp->desc.p, n, chunks, vtot, max_rows, grp->sc, grp->work.p, d_res, false, ctx->tuned, s,
+                        nullptr, nullptr, halo_parts);
+}
+
+}  // namespace
+
+extern "C" {
+
 int tc_count_parts_csr_i32(tc_ctx *ctx, int n_parts, const int32_t *const *row_ptrs, const int32_t *const *cols,
                            const int64_t *n_rows, const int64_t *nnz, const int64_t *n_roots, uint64_t *outs,
                            uint64_t *total) {
@@ -1043,10 +1113,14 @@ int tc_count_parts_csr_i32(tc_ctx *ctx, int n_parts, const int32_t *const *row_p
     // Three streams: every part's upload goes out on the copy stream at once;
     // part p is validated on the (high-priority) validation stream as soon as
     // its upload lands.  A few large parts (at most 64, 4 M entries each on
-    // average; the parts of one graph) are then counted one launch each on
-    // the context's stream while the later parts are still being uploaded --
-    // the copy engine and the SMs work at the same time (R-MAT 23's eight
-    // parts: 3.3 GB of uploads under 43 ms of counts).  Many small graphs are
+    // average; the parts of one graph) are then counted on the context's
+    // stream while the later parts are still being uploaded -- the copy
+    // engine and the SMs work at the same time (R-MAT 23's eight parts: 3.3 GB
+    // of uploads in 16 ms under 41 ms of counts) -- in groups of 1, 2, 4, ...
+    // parts, one pooled launch per group (the last group takes the rest once
+    // fewer than half the next group's size would be left): part 0 starts as
+    // soon as it is in, and the later groups pay one launch tail and one
+    // validation gap each instead of one per part.  Many small graphs are
     // counted together in one batched launch once all are in (one launch each
     // would cost more than the copies).  The host waits only for verdicts.
     if (!ctx->aux[0]) {
@@ -1067,6 +1141,15 @@ int tc_count_parts_csr_i32(tc_ctx *ctx, int n_parts, const int32_t *const *row_p
         sum_nnz += nnz[p];
     }
     const bool overlap = n_parts <= 64 && sum_nnz / n_parts >= ((int64_t)1 << 22);
+    std::vector<int> group_end;  // exclusive ends of the overlapped groups
+    for (int a = 0, sz = 1; overlap && a < n_parts; a = group_end.back(), sz *= 2) {
+        int b = std::min(n_parts, a + sz);
+        if (n_parts - b < sz) b = n_parts;
+        group_end.push_back(b);
+    }
+    std::vector<std::unique_ptr<PartGroup>> groups;
+    size_t next_group = 0;
+    int group_start = 0;
     int st = d_res.alloc((size_t)n_parts, S);
     if (st == TC_OK && cudaMemsetAsync(d_res.p, 0, sizeof(unsigned long long) * (size_t)n_parts, S) != cudaSuccess)
         st = set_error(TC_E_CUDA, "result memset failed");
@@ -1104,7 +1187,17 @@ int tc_count_parts_csr_i32(tc_ctx *ctx, int n_parts, const int32_t *const *row_p
             break;
         }
         if (cudaStreamWaitEvent(S, copied[(size_t)p], 0) != cudaSuccess) st = set_error(TC_E_CUDA, "event wait failed");
-        if (st == TC_OK && overlap) st = enqueue_graph_count(g, nullptr, d_res.p + p, nullptr);
+        if (st == TC_OK && overlap && p + 1 == group_end[next_group]) {  // the group is in and valid
+            if (p == group_start) {
+                st = enqueue_graph_count(g, nullptr, d_res.p + p, nullptr);
+            } else {
+                groups.push_back(std::make_unique<PartGroup>());
+                st = enqueue_group_count(ctx, gs.data() + group_start, p + 1 - group_start, d_res.p + group_start,
+                                         groups.back().get());
+            }
+            group_start = p + 1;
+            ++next_group;
+        }
     }
     std::vector<unsigned long long> h_res((size_t)n_parts, 0);
     int bad = 0;
@@ -1121,7 +1214,7 @@ int tc_count_parts_csr_i32(tc_ctx *ctx, int n_parts, const int32_t *const *row_p
     cudaStreamSynchronize(Cs);
     cudaStreamSynchronize(Vs);
     if (cudaStreamSynchronize(S) != cudaSuccess && st == TC_OK) st = set_error(TC_E_CUDA, "parts count failed");
-    for (int p = 0; p < n_parts && st == TC_OK && overlap; ++p) {
+    for (int p = 0; p < n_parts && st == TC_OK && overlap; ++p) {  // parts counted on their own
         tc_graph *g = gs[(size_t)p];
         if (g->d_work) {
             CountWork w;
@@ -1129,6 +1222,12 @@ int tc_count_parts_csr_i32(tc_ctx *ctx, int n_parts, const int32_t *const *row_p
             else if (w.error) bad = w.error;
         }
     }
+    for (size_t i = 0; i < groups.size() && st == TC_OK; ++i) {  // the pooled launches
+        CountWork w;
+        if (cudaMemcpy(&w, groups[i]->work.p, sizeof w, cudaMemcpyDeviceToHost) != cudaSuccess) bad = -1;
+        else if (w.error) bad = w.error;
+    }
+    groups.clear();
     if (st == TC_OK && bad > 0) st = set_error(TC_E_STATE, "%s", count_error_text(bad));
     if (st == TC_OK && bad < 0) st = set_error(TC_E_CUDA, "work word read-back failed");
     for (auto &e : copied)
