@@ -78,7 +78,9 @@ constexpr int kHeavyChunk = 16; // partners per warp grab inside a heavy unit (4
 constexpr int kLaneRowDeg = 16; // auxiliary passes: rows with d+ <= this are walked one per lane
 constexpr int kMicroDeg = 8;    // micro tasks: d+(x) <= this (N+(x) held in registers) ...
 constexpr int kMicroWork = 128; // ... and at most this many probes (one lane runs the task serially)
-constexpr int kAuxGrab = 4;     // 32-row chunks an auxiliary-kernel warp takes per cursor grab
+constexpr int kAuxGrab = 2;     // 32-row chunks an auxiliary-kernel warp takes per cursor grab (4 -> 2:
+                                // R-MAT 23's eight parts 40.65 -> 40.50 ms, R-MAT 21's 8.43 -> 8.26 ms, the
+                                // 256-graph batch unchanged; 1 costs that batch 3 %, 8 costs the parts 2.5 %)
 // One middle-centric in-edge in a packed in_work word.  Both halves stay below
 // 2^31: a vertex has fewer than nnz in-edges, and its in-partners' d+(u) sum to
 // at most nnz < 2^31 (each u counted once), so one 64-bit atomic adds both.
