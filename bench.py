@@ -787,6 +787,7 @@ def run_parts(args, world, rank, local, pg):
             "e2e": {"value": E / (e2e / 1000.0) if e2e else None, "unit": UNIT, "ms_per_step": e2e,
                     "ms_min": min(e2e_ms) if e2e_ms else None,
                     "ms_median": sorted(e2e_ms)[len(e2e_ms) // 2] if e2e_ms else None,
+                    "ms_steps": [round(x, 2) for x in e2e_ms],
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 20 * len(pinned) + 48,
                     "path": "tc_count_parts_csr_i32: every part's upload issued at once; each part validated as "
                             "soon as it is in; the parts counted in groups of 1, 2, then the rest, one launch per "

@@ -138,12 +138,6 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
                          const CountScratch &sc, int32_t *scan_tmp, int64_t scan_tmp_cap, CountWork *work,
                          unsigned long long *results, const Tuned &tn, cudaStream_t s);
 
-// Enqueues classify + persistent count for n_graphs descriptors on stream s.
-// results[n_graphs] receives the per-graph totals (zeroed here).
-// Enqueues [in_count -> scan -> transpose/classify -> count] for n_graphs
-// descriptors on stream s; total_vertices = sum (n_rows + 1).
-// max_rows = largest n_rows among the graphs.  kev (optional, two events) is
-// recorded around the counting kernels (heavy bitmap + persistent count).
 // One-kernel count of a graph whose rows are all at most max_deg <= 8 long
 // (one lane per root, lists in registers); fills the work words and result
 // like launch_count.
@@ -151,8 +145,13 @@ int launch_flat(const int32_t *rp, const int32_t *col, int64_t n_roots, int max_
                 unsigned long long *result, unsigned long long *per_root, const Tuned &tn, cudaStream_t s,
                 int *launches, cudaEvent_t *kev);
 
-// halo_parts: some graph of the launch is a halo part (n_roots < n_rows); its
-// heavy units then run the count kernel's instance for small units.
+// Enqueues [degree -> in_count -> scan -> transpose/classify -> micro ->
+// count] for n_graphs descriptors on stream s; results[n_graphs] receives the
+// per-graph totals (zeroed here); total_vertices = sum (n_rows + 1), max_rows
+// = the largest n_rows.  kev (optional, two events) is recorded around the
+// counting kernels (heavy bitmap + persistent count).  halo_parts: some graph
+// of the launch is a halo part (n_roots < n_rows); its heavy units then run
+// the count kernel's instance for small units.
 int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, int64_t total_vertices,
                  int64_t max_rows, const CountScratch &sc, CountWork *work, unsigned long long *results, bool per_root,
                  const Tuned &tn, cudaStream_t s, int *launches, cudaEvent_t *kev = nullptr,
