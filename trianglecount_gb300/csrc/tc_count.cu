@@ -1149,7 +1149,19 @@ __global__ void __launch_bounds__(kBigThreads, 1) heavy_bitmap_kernel(KParams P,
 // unit while the other warps finish the current one (below).  Whole graphs
 // get the instance without either: the same rules cost them 2-3 % (R-MAT 21
 // 6.03 -> 6.21 ms, R-MAT 23 33.8 -> 34.6 ms) even where they never fire.
-template <bool kPerRoot, bool kPairsOnly, bool kStage = false, bool kParts = false>
+// kPhases: 3 = both phases in one kernel, 1 = phase A only (heavy units),
+// 2 = phase B only (light tasks).  Launches with halo parts run the two
+// phases as two kernels, each with its own register allocation: in one
+// kernel, phase B's live values made the halo-part instance spill 108 bytes
+// at 40 registers and its phase A ran ~2 ms slower on R-MAT 23's eight parts
+// (per-block %globaltimer stamps: phase A ended at 33.9 ms with phase B in
+// the kernel, 31.8 ms without); split, those parts count in 38.09 instead of
+// 40.47 ms and R-MAT 21's in 7.89 instead of 8.26.  Whole graphs keep one
+// kernel: there the blocks that finish phase A early fill its tail with light
+// tasks, which two kernels cannot (R-MAT 21 6.65 -> 7.08 ms split).  Light
+// tasks do not depend on heavy units (the totals are atomic adds), so only
+// the schedule differs.
+template <bool kPerRoot, bool kPairsOnly, bool kStage = false, bool kParts = false, int kPhases = 3>
 __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KParams P) {
     extern __shared__ __align__(16) int smem[];
     __shared__ unsigned s_unit;
@@ -1228,8 +1240,8 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
             if (!kParts) s_chunk = 0;
         }
     };
-    if (kParts && !P.heavy_done && warp == 0) grab_next();
-    for (; !P.heavy_done;) {
+    if (kParts && (kPhases & 1) && !P.heavy_done && warp == 0) grab_next();
+    for (; (kPhases & 1) && !P.heavy_done;) {
         if (!kParts && warp == 0) grab_next();
         __syncthreads();  // this unit's s_unit / s_entry are set (and the last unit's probes are done)
         const unsigned unit = s_unit;
@@ -1341,7 +1353,7 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
     // last tasks of the kernel are single tasks, not whole 32-row chunks.
     int *wtab = smem + warp * (1 << P.log_warp_slots);
     const unsigned n_light = (unsigned)P.work->n_tasks;
-    for (;;) {
+    for (; kPhases & 2;) {
         unsigned t0 = 0;
         if (lane == 0) t0 = atomicAdd(&P.work->small_cursor, (unsigned)(kParts ? 8 : kLightGrab));
         t0 = __shfl_sync(kFull, t0, 0);
@@ -1435,6 +1447,40 @@ __global__ void __launch_bounds__(kThreads, TC_COUNT_MIN_BLOCKS) count_kernel(KP
     if (!kPerRoot) flush(-1);
 }
 
+// Dynamic shared memory of the kernels launch_phases runs for one instance.
+template <bool kPerRoot, bool kPairsOnly, bool kStage = false, bool kParts = false>
+int set_count_smem(size_t smem) {
+    if constexpr (!kParts) {
+        TC_CUDA(cudaFuncSetAttribute(count_kernel<kPerRoot, kPairsOnly, kStage, kParts, 3>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    } else {
+        TC_CUDA(cudaFuncSetAttribute(count_kernel<kPerRoot, kPairsOnly, kStage, kParts, 1>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        TC_CUDA(cudaFuncSetAttribute(count_kernel<kPerRoot, kPairsOnly, kStage, kParts, 2>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    return TC_OK;
+}
+
+// The count of one instance on s: one kernel for both phases, or (halo
+// parts) phase A's kernel -- unless the bitmap kernel took the heavy units --
+// and then phase B's; returns the launches.
+template <bool kPerRoot, bool kPairsOnly, bool kStage = false, bool kParts = false>
+int launch_phases(const KParams &P, const Tuned &tn, cudaStream_t s) {
+    if constexpr (!kParts) {
+        count_kernel<kPerRoot, kPairsOnly, kStage, kParts, 3><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        return 1;
+    } else {
+        int n = 0;
+        if (!P.heavy_done) {
+            count_kernel<kPerRoot, kPairsOnly, kStage, kParts, 1><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+            ++n;
+        }
+        count_kernel<kPerRoot, kPairsOnly, kStage, kParts, 2><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        return n + 1;
+    }
+}
+
 int pow2_floor_log(int x) {
     int l = 0;
     while ((2 << l) <= x) ++l;
@@ -1487,18 +1533,14 @@ int resolve_tuning(const tc_tuning &t, int sm_count, Tuned *out) {
     if (r.long_list > 4096) return set_error(TC_E_INVALID, "long_list must be <= 4096, got %d", r.long_list);
     r.threads = kThreads;
     r.smem = (size_t)block_slots * sizeof(int);
-    TC_CUDA(cudaFuncSetAttribute(count_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
-    TC_CUDA(cudaFuncSetAttribute(count_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
-    TC_CUDA(cudaFuncSetAttribute(count_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
-    TC_CUDA(cudaFuncSetAttribute(count_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.smem));
-    TC_CUDA(cudaFuncSetAttribute(count_kernel<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)r.smem));
-    TC_CUDA(cudaFuncSetAttribute(count_kernel<false, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)r.smem));
-    TC_CUDA(cudaFuncSetAttribute(count_kernel<true, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)r.smem));
-    TC_CUDA(cudaFuncSetAttribute(count_kernel<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)r.smem));
+    TC_TRY((set_count_smem<false, false>(r.smem)));
+    TC_TRY((set_count_smem<true, false>(r.smem)));
+    TC_TRY((set_count_smem<false, true>(r.smem)));
+    TC_TRY((set_count_smem<true, true>(r.smem)));
+    TC_TRY((set_count_smem<false, false, true>(r.smem)));
+    TC_TRY((set_count_smem<true, false, true>(r.smem)));
+    TC_TRY((set_count_smem<false, false, false, true>(r.smem)));
+    TC_TRY((set_count_smem<true, false, false, true>(r.smem)));
     int occ = 0;
     TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, count_kernel<false, false>, kThreads, r.smem));
     if (occ < 1) return set_error(TC_E_INVALID, "count kernel does not fit on an SM with %zu B shared memory", r.smem);
@@ -1604,19 +1646,19 @@ int launch_count(const GraphDesc *d_desc, int n_graphs, int64_t total_chunks, in
             ++nl;
         }
         if (per_root) {
-            if (tn.hash_pairs) count_kernel<true, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
-            else if (P.intersect) count_kernel<true, false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
-            else if (halo_parts) count_kernel<true, false, false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
-            else count_kernel<true, false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+            if (tn.hash_pairs) nl += launch_phases<true, true>(P, tn, s);
+            else if (P.intersect) nl += launch_phases<true, false, true>(P, tn, s);
+            else if (halo_parts) nl += launch_phases<true, false, false, true>(P, tn, s);
+            else nl += launch_phases<true, false>(P, tn, s);
         } else {
-            if (tn.hash_pairs) count_kernel<false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
-            else if (P.intersect) count_kernel<false, false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
-            else if (halo_parts) count_kernel<false, false, false, true><<<tn.blocks, kThreads, tn.smem, s>>>(P);
-            else count_kernel<false, false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+            if (tn.hash_pairs) nl += launch_phases<false, true>(P, tn, s);
+            else if (P.intersect) nl += launch_phases<false, false, true>(P, tn, s);
+            else if (halo_parts) nl += launch_phases<false, false, false, true>(P, tn, s);
+            else nl += launch_phases<false, false>(P, tn, s);
         }
         if (kev) TC_TRY(record_kernel_event(kev[1], s));
         TC_CUDA(cudaGetLastError());
-        nl += 5 + scan_launches(total_vertices);
+        nl += 4 + scan_launches(total_vertices);
     }
     if (launches) *launches = nl;
     return TC_OK;
@@ -1697,7 +1739,7 @@ int launch_count_noalloc(const GraphDesc *d_desc, int64_t total_chunks, int64_t 
         transpose_classify_kernel<<<aux_blocks, kThreads, 0, s>>>(P, sc.heavy);
         TC_CUDA(cudaGetLastError());
         micro_kernel<false><<<aux_blocks, kThreads, 0, s>>>(P);
-        count_kernel<false, false><<<tn.blocks, kThreads, tn.smem, s>>>(P);
+        launch_phases<false, false>(P, tn, s);
         TC_CUDA(cudaGetLastError());
     }
     return TC_OK;
