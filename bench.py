@@ -746,7 +746,7 @@ def run_parts(args, world, rank, local, pg):
     sec = k_ms / 1000.0
     roofline = {"bound": "hbm", "achieved": B_min / sec / 1e9, "peak": peak, "unit": "GB/s",
                 "frac": B_min / sec / 1e9 / peak, "traffic": traffic,
-                "peak_source": f"{peak_src} hbm_gbs (copy, burst)", "kernel": "count_kernel (batched, k = 8 parts)",
+                "peak_source": f"{peak_src} hbm_gbs (copy, burst)", "kernel": "count_kernel, the batched k = 8 count's two phase kernels (heavy units, then light tasks)",
                 "kernel_ms": k_ms, "algorithmic_bytes_per_launch": B_min,
                 "algorithmic_bytes_definition": "sum over parts of 4(R+1) + 12 E_R + 4 sum_{u->v} min(d+(u), d+(v)) "
                                                 "+ 8 (R roots, E_R root edges): each root's row_ptr and list, each "
