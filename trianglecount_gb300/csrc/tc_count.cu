@@ -51,6 +51,8 @@
 //                  slice from a shared cursor;
 //                phase B -- warps take light tasks four at a time from the
 //                  list and run each with a per-warp shared hash.
+//              A launch with halo parts runs the two phases as two kernels
+//              (each with its own register allocation).
 //              Streaming a chunk of partners: lists with length >= long_list are
 //              read by the whole warp, four coalesced loads in flight per lane;
 //              shorter lists are flattened across the lanes (warp scan of the
