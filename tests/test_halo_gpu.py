@@ -109,3 +109,44 @@ def test_counting_halo_tie_breaks(ctx, tie):
         assert np.array_equal(drp, lrp) and np.array_equal(dcol, lcol), (tie, p)
         total += ctx.count(g)
     assert total == whole
+
+
+PART_TUNINGS = [
+    {},  # defaults: the halo-part instance, heavy and light phases as two kernels
+    {"warp_max_deg": 32, "light_max_work": 1, "unit_work": 1, "long_list": 0},  # heavy units everywhere
+    {"warp_max_deg": 512, "light_max_work": 1 << 30, "unit_work": 1 << 30, "long_list": 4096},  # warps only
+    {"heavy_bitmap": 1, "warp_max_deg": 32, "light_max_work": 64},  # heavy units on the bitmap kernel
+    {"intersect": 1, "warp_max_deg": 32, "light_max_work": 64},  # sorted lists, bulk-staged
+]
+
+
+@pytest.mark.parametrize("tuning", PART_TUNINGS)
+def test_halo_parts_per_root_match_oracle(ctx, tuning):
+    """Per-root counts (the reference's g_sum) of halo parts, through the
+    halo-part instance's two phase kernels under tunings that send the work to
+    heavy units, to warps only, to the bitmap kernel or to sorted lists: each
+    part's per-root array equals the oracle's, its total equals the plain
+    count, and a batch of the parts agrees."""
+    old = ctx.get_tuning()
+    try:
+        ctx.set_tuning(**tuning)
+        src, dst = gen.rmat(13)
+        rp, col = oracle.clean(src, dst)
+        deg = np.diff(rp)
+        whole = oracle.count(*oracle.orient(rp, col))
+        part = gen.parts_random(len(rp) - 1, 4)
+        ug = ctx.upload_ugraph(rp, col, deg)
+        for mode in ("reference", "count"):
+            parts = ctx.halo_extract(ug, part, 4, mode=mode)
+            total = 0
+            for p, g in enumerate(parts):
+                lrp, lcol, t_ver = oracle.halo_part(rp, col, deg, part, p, mode=mode)
+                want, want_pr = oracle.count(lrp, lcol, n_roots=t_ver, per_root=True)
+                got_pr = ctx.count_per_root(g)
+                assert len(got_pr) == t_ver and np.array_equal(got_pr, want_pr), (mode, p)
+                assert ctx.count(g) == want == int(got_pr.sum())
+                total += want
+            assert total == whole
+            assert list(ctx.batch(parts).run()) == [int(ctx.count(g)) for g in parts]
+    finally:
+        ctx.set_tuning(**old)
