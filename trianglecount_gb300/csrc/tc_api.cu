@@ -1213,7 +1213,7 @@ int tc_count_parts_csr_i32(tc_ctx *ctx, int n_parts, const int32_t *const *row_p
             break;
         }
         if (cudaStreamWaitEvent(S, copied[(size_t)p], 0) != cudaSuccess) st = set_error(TC_E_CUDA, "event wait failed");
-        if (st == TC_OK && overlap && p + 1 == group_end[next_group]) {  // the group is in and valid
+        if (st == TC_OK && p + 1 == group_end[next_group]) {  // the group is in and valid
             if (p == group_start) {
                 st = enqueue_graph_count(g, nullptr, d_res.p + p, nullptr);
             } else {
